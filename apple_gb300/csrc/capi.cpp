@@ -1,0 +1,777 @@
+// C ABI of apple_gb300: handle lifetimes, uploads and launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "agb_internal.h"
+#include "kernels.h"
+#include "solver.h"
+
+namespace agb {
+const char* last_error();
+}
+
+using namespace agb;
+
+namespace {
+
+template <class T>
+int dalloc(T** p, size_t n) {
+  *p = nullptr;
+  AGB_CHECK_CUDA(cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T)));
+  return AGB_OK;
+}
+
+int dalloc_bytes(void** p, size_t bytes) {
+  *p = nullptr;
+  AGB_CHECK_CUDA(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+  return AGB_OK;
+}
+
+int upload(void* d, const void* h, size_t bytes) {
+  if (bytes == 0) return AGB_OK;
+  AGB_CHECK_CUDA(cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice));
+  return AGB_OK;
+}
+
+template <class T>
+int dupload(T** d, const std::vector<T>& h) {
+  int rc = dalloc(d, h.size());
+  if (rc) return rc;
+  return upload(*d, h.data(), h.size() * sizeof(T));
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+#define RC(call)           \
+  do {                     \
+    int rc_ = (call);      \
+    if (rc_) return rc_;   \
+  } while (0)
+
+// element records of a plan in the kernels' layout
+int upload_records(const TilePlan& plan, int precision, void** d_rec, uint32_t** d_ids) {
+  const size_t n = (size_t)plan.n_cells;
+  *d_ids = nullptr;
+  if (precision == AGB_F32) {
+    std::vector<float> rec(12 * n);
+    for (size_t e = 0; e < n; ++e) {
+      float* A = &rec[4 * e];
+      float* B = &rec[4 * (n + e)];
+      float* C = &rec[4 * (2 * n + e)];
+      for (int k = 0; k < 4; ++k) A[k] = (float)plan.D[k * n + e];
+      for (int k = 0; k < 4; ++k) B[k] = (float)plan.D[(4 + k) * n + e];
+      C[0] = (float)plan.D[8 * n + e];
+      C[1] = (float)plan.mudv[e];
+      C[2] = (float)plan.lamdv[e];
+      std::memcpy(&C[3], &plan.ids[e], 4);
+    }
+    RC(dalloc_bytes(d_rec, rec.size() * sizeof(float)));
+    return upload(*d_rec, rec.data(), rec.size() * sizeof(float));
+  }
+  std::vector<double> rec(11 * n);
+  for (size_t k = 0; k < 9; ++k)
+    std::memcpy(&rec[k * n], &plan.D[k * n], n * sizeof(double));
+  std::memcpy(&rec[9 * n], plan.mudv.data(), n * sizeof(double));
+  std::memcpy(&rec[10 * n], plan.lamdv.data(), n * sizeof(double));
+  RC(dalloc_bytes(d_rec, rec.size() * sizeof(double)));
+  RC(upload(*d_rec, rec.data(), rec.size() * sizeof(double)));
+  return dupload(d_ids, plan.ids);
+}
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int check_launch(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return AGB_E_CUDA;
+  }
+  return AGB_OK;
+}
+
+template <class R>
+std::vector<R> pack_v4(const std::vector<double>& xyz, const std::vector<uint8_t>* mask) {
+  const size_t n = xyz.size() / 3;
+  std::vector<R> out(4 * n);
+  for (size_t i = 0; i < n; ++i) {
+    for (int c = 0; c < 3; ++c) out[4 * i + c] = (R)xyz[3 * i + c];
+    out[4 * i + 3] = mask ? (R)(*mask)[i] : R(0);
+  }
+  return out;
+}
+
+}  // namespace
+
+FemView agb_fem::view() const {
+  FemView v{};
+  v.material = material;
+  v.n_tiles = plan.n_tiles;
+  v.n_cells = plan.n_cells;
+  v.tile_estart = d_tile_estart;
+  v.tile_vstart = d_tile_vstart;
+  v.tv_vid = d_tv_vid;
+  v.rec = d_rec;
+  v.ids = d_ids;
+  return v;
+}
+
+extern "C" {
+
+const char* agb_last_error(void) { return agb::last_error(); }
+const char* agb_version(void) { return "apple_gb300 0.1.0 (sm_103a)"; }
+
+// ---------------------------------------------------------------------------
+// space
+// ---------------------------------------------------------------------------
+int agb_space_create(int32_t n_points, const double* points, agb_space** out) {
+  AGB_REQUIRE(out && n_points >= 0, AGB_E_INVALID, "agb_space_create: bad arguments");
+  *out = nullptr;
+  agb_space* s = new (std::nothrow) agb_space();
+  AGB_REQUIRE(s, AGB_E_INVALID, "agb_space_create: out of host memory");
+  s->n_points = n_points;
+  if (points) {
+    s->user_of_internal = morton_order(n_points, points);
+    s->points_internal.resize(3 * (size_t)n_points);
+    for (int i = 0; i < n_points; ++i)
+      for (int c = 0; c < 3; ++c) s->points_internal[3 * i + c] = points[3 * s->user_of_internal[i] + c];
+  } else {
+    s->user_of_internal.resize(n_points);
+    for (int i = 0; i < n_points; ++i) s->user_of_internal[i] = i;
+  }
+  s->internal_of_user.resize(n_points);
+  for (int i = 0; i < n_points; ++i) s->internal_of_user[s->user_of_internal[i]] = i;
+  int rc = dupload(&s->d_user_of_internal, s->user_of_internal);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return AGB_OK;
+}
+
+int agb_space_destroy(agb_space* s) {
+  if (!s) return AGB_OK;
+  dfree(s->d_user_of_internal);
+  delete s;
+  return AGB_OK;
+}
+
+int agb_space_order(const agb_space* s, int32_t* internal_of_user) {
+  AGB_REQUIRE(s && internal_of_user, AGB_E_INVALID, "agb_space_order: null argument");
+  std::memcpy(internal_of_user, s->internal_of_user.data(), sizeof(int32_t) * s->n_points);
+  return AGB_OK;
+}
+
+int agb_region_compute(int32_t n_cells, const int32_t* cells, int32_t n_points,
+                       const double* points, const double* fraction, double* dhdX, double* dV,
+                       int32_t* n_nonpositive) {
+  AGB_REQUIRE(n_cells >= 0 && (n_cells == 0 || (cells && points && dhdX && dV)), AGB_E_INVALID,
+              "agb_region_compute: null argument");
+  for (int64_t k = 0; k < 4 * (int64_t)n_cells; ++k)
+    AGB_REQUIRE(cells[k] >= 0 && cells[k] < n_points, AGB_E_MESH,
+                "agb_region_compute: point id %d outside [0, %d)", cells[k], n_points);
+  std::vector<double> D9(9 * (size_t)n_cells);
+  const int bad = region_compute(n_cells, cells, points, fraction, D9.data(), dV);
+  for (int e = 0; e < n_cells; ++e) {
+    double* row = dhdX + 12 * (size_t)e;
+    for (int j = 0; j < 3; ++j) {
+      row[3 + j] = D9[9 * (size_t)e + j];
+      row[6 + j] = D9[9 * (size_t)e + 3 + j];
+      row[9 + j] = D9[9 * (size_t)e + 6 + j];
+      row[j] = -(row[3 + j] + row[6 + j] + row[9 + j]);
+    }
+  }
+  if (n_nonpositive) *n_nonpositive = bad;
+  return AGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FEM potential
+// ---------------------------------------------------------------------------
+int agb_fem_destroy(agb_fem* f) {
+  if (!f) return AGB_OK;
+  for (void* p : {(void*)f->d_tile_estart, (void*)f->d_tile_vstart, (void*)f->d_tv_vid,
+                  (void*)f->d_own_slot, (void*)f->d_own_off, f->d_rec, (void*)f->d_ids, f->d_u,
+                  f->d_p, f->d_slots, (void*)f->d_partials, (void*)f->d_counter})
+    dfree(p);
+  delete f;
+  return AGB_OK;
+}
+
+int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cells,
+                   const int32_t* cells, const double* points, const double* dhdX,
+                   const double* dV, const double* fraction, const double* mu,
+                   const double* lambda, int32_t tile_elems, agb_fem** out) {
+  AGB_REQUIRE(out, AGB_E_INVALID, "agb_fem_create: out is null");
+  *out = nullptr;
+  AGB_REQUIRE(space, AGB_E_INVALID, "agb_fem_create: space is null");
+  AGB_REQUIRE(material == AGB_ARAP || material == AGB_STABLE_NEO_HOOKEAN, AGB_E_INVALID,
+              "agb_fem_create: unknown material %d", material);
+  AGB_REQUIRE(precision == AGB_F32 || precision == AGB_F64, AGB_E_INVALID,
+              "agb_fem_create: unknown precision %d", precision);
+  AGB_REQUIRE(n_cells >= 0 && (n_cells == 0 || cells), AGB_E_INVALID, "agb_fem_create: cells");
+  AGB_REQUIRE(mu || n_cells == 0, AGB_E_INVALID, "agb_fem_create: mu is null");
+  AGB_REQUIRE(material == AGB_ARAP || lambda || n_cells == 0, AGB_E_INVALID,
+              "agb_fem_create: lambda is null for stable Neo-Hookean");
+  const int np = space->n_points;
+  for (int64_t k = 0; k < 4 * (int64_t)n_cells; ++k)
+    AGB_REQUIRE(cells[k] >= 0 && cells[k] < np, AGB_E_MESH,
+                "agb_fem_create: cell %lld corner %lld has point id %d outside [0, %d)",
+                (long long)(k / 4), (long long)(k % 4), cells[k], np);
+  const double* pts_user = points;
+  std::vector<double> pts_from_space;
+  if (!pts_user && !space->points_internal.empty()) {
+    pts_from_space.resize(3 * (size_t)np);
+    for (int i = 0; i < np; ++i)
+      for (int c = 0; c < 3; ++c)
+        pts_from_space[3 * space->user_of_internal[i] + c] = space->points_internal[3 * i + c];
+    pts_user = pts_from_space.data();
+  }
+  AGB_REQUIRE((dhdX && dV) || pts_user, AGB_E_INVALID,
+              "agb_fem_create: need dhdX and dV, or rest positions");
+
+  std::vector<double> D9(9 * (size_t)n_cells), vol(n_cells);
+  if (pts_user && (!dhdX || !dV)) {
+    std::vector<double> d9c(9 * (size_t)n_cells), vc(n_cells);
+    region_compute(n_cells, cells, pts_user, nullptr, d9c.data(), vc.data());
+    if (!dhdX) D9 = d9c;
+    if (!dV) vol = vc;
+  }
+  if (dhdX)
+    for (int e = 0; e < n_cells; ++e)
+      for (int k = 0; k < 9; ++k) D9[9 * (size_t)e + k] = dhdX[12 * (size_t)e + 3 + k];
+  if (dV)
+    for (int e = 0; e < n_cells; ++e) vol[e] = dV[e];
+  if (fraction)
+    for (int e = 0; e < n_cells; ++e) vol[e] *= fraction[e];
+  std::vector<double> mudv(n_cells), lamdv(n_cells, 0.0);
+  for (int e = 0; e < n_cells; ++e) {
+    mudv[e] = mu[e] * vol[e];
+    if (lambda && material == AGB_STABLE_NEO_HOOKEAN) lamdv[e] = lambda[e] * vol[e];
+  }
+  std::vector<int32_t> cells_int(4 * (size_t)n_cells);
+  for (size_t k = 0; k < cells_int.size(); ++k) cells_int[k] = space->internal_of_user[cells[k]];
+  std::vector<double> centroid(3 * (size_t)n_cells);
+  for (int e = 0; e < n_cells; ++e)
+    for (int c = 0; c < 3; ++c) {
+      double s = 0.0;
+      for (int a = 0; a < 4; ++a)
+        s += pts_user ? pts_user[3 * (size_t)cells[4 * e + a] + c]
+                      : (c == 0 ? (double)cells_int[4 * e + a] : 0.0);
+      centroid[3 * (size_t)e + c] = 0.25 * s;
+    }
+
+  agb_fem* f = new (std::nothrow) agb_fem();
+  AGB_REQUIRE(f, AGB_E_INVALID, "agb_fem_create: out of host memory");
+  f->space = space;
+  f->material = material;
+  f->precision = precision;
+  int rc = build_tiles(n_cells, cells_int.data(), centroid.data(), D9.data(), mudv.data(),
+                       lamdv.data(), tile_elems, &f->plan);
+  std::vector<SlotMap> sm;
+  if (!rc) {
+    build_slots(np, {&f->plan}, &sm, &f->own_off);
+    f->own_slots = sm[0];
+  }
+  const TilePlan& P = f->plan;
+  const size_t v4 = v4_bytes(precision);
+  const size_t n_part = (size_t)std::max(P.n_tiles, unpack_blocks(np)) * 2;
+  if (!rc) rc = dupload(&f->d_tile_estart, P.tile_estart);
+  if (!rc) rc = dupload(&f->d_tile_vstart, P.tile_vstart);
+  if (!rc) rc = dupload(&f->d_tv_vid, P.tv_vid);
+  if (!rc) rc = dupload(&f->d_own_slot, f->own_slots.slot_of_tv);
+  if (!rc) rc = dupload(&f->d_own_off, f->own_off);
+  if (!rc) rc = upload_records(P, precision, &f->d_rec, &f->d_ids);
+  if (!rc) rc = dalloc_bytes(&f->d_u, v4 * np);
+  if (!rc) rc = dalloc_bytes(&f->d_p, v4 * np);
+  if (!rc) rc = dalloc_bytes(&f->d_slots, v4 * 3 * (size_t)P.n_tv);
+  if (!rc) rc = dalloc(&f->d_partials, n_part);
+  if (!rc) rc = dalloc(&f->d_counter, 1);
+  if (!rc && cudaMemset(f->d_counter, 0, sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
+  if (rc) {
+    agb_fem_destroy(f);
+    return rc;
+  }
+  *out = f;
+  return AGB_OK;
+}
+
+int agb_fem_info(const agb_fem* f, int32_t* n_tiles, int32_t* n_tv) {
+  AGB_REQUIRE(f, AGB_E_INVALID, "agb_fem_info: null handle");
+  if (n_tiles) *n_tiles = f->plan.n_tiles;
+  if (n_tv) *n_tv = f->plan.n_tv;
+  return AGB_OK;
+}
+
+int agb_fem_eval(agb_fem* f, unsigned flags, const void* u, const void* p, double* energy,
+                 void* grad, void* diag, void* prod, double* quad, void* stream) {
+  AGB_REQUIRE(f && u, AGB_E_INVALID, "agb_fem_eval: null handle or u");
+  AGB_REQUIRE(!(flags & ~31u), AGB_E_INVALID, "agb_fem_eval: unknown flags %u", flags);
+  AGB_REQUIRE(!(flags & AGB_FUN) || energy, AGB_E_INVALID, "agb_fem_eval: energy output is null");
+  AGB_REQUIRE(!(flags & AGB_GRAD) || grad, AGB_E_INVALID, "agb_fem_eval: grad output is null");
+  AGB_REQUIRE(!(flags & AGB_HESS_DIAG) || diag, AGB_E_INVALID, "agb_fem_eval: hess_diag output is null");
+  AGB_REQUIRE(!(flags & AGB_HESS_PROD) || prod, AGB_E_INVALID, "agb_fem_eval: hess_prod output is null");
+  AGB_REQUIRE(!(flags & AGB_HESS_QUAD) || quad, AGB_E_INVALID, "agb_fem_eval: hess_quad output is null");
+  const bool need_p = flags & (AGB_HESS_PROD | AGB_HESS_QUAD);
+  AGB_REQUIRE(!need_p || p, AGB_E_INVALID, "agb_fem_eval: p is null");
+  if (!flags) return AGB_OK;
+  cudaStream_t s = as_stream(stream);
+  const int np = f->space->n_points;
+  RC(check_launch(launch_pack(f->precision, np, f->space->d_user_of_internal, u, f->d_u,
+                              need_p ? p : nullptr, f->d_p, s),
+                  "pack"));
+  RC(check_launch(launch_fem_eval(f->precision, f->view(), flags, f->d_u, f->d_p, f->d_own_slot,
+                                  f->d_slots, f->plan.n_tv, f->d_partials, f->d_counter, energy,
+                                  quad, s),
+                  "fem_eval"));
+  const unsigned vec = flags & (AGB_GRAD | AGB_HESS_DIAG | AGB_HESS_PROD);
+  if (vec)
+    RC(check_launch(launch_unpack(f->precision, np, f->space->d_user_of_internal, f->d_own_off,
+                                  f->d_slots, f->plan.n_tv, vec, grad, diag, prod, nullptr,
+                                  f->d_u, f->d_partials, f->d_counter, nullptr, s),
+                    "unpack"));
+  return AGB_OK;
+}
+
+int agb_fem_fun(agb_fem* f, const void* u, double* out, void* s) {
+  return agb_fem_eval(f, AGB_FUN, u, nullptr, out, nullptr, nullptr, nullptr, nullptr, s);
+}
+int agb_fem_grad(agb_fem* f, const void* u, void* out, void* s) {
+  return agb_fem_eval(f, AGB_GRAD, u, nullptr, nullptr, out, nullptr, nullptr, nullptr, s);
+}
+int agb_fem_hess_diag(agb_fem* f, const void* u, void* out, void* s) {
+  return agb_fem_eval(f, AGB_HESS_DIAG, u, nullptr, nullptr, nullptr, out, nullptr, nullptr, s);
+}
+int agb_fem_hess_prod(agb_fem* f, const void* u, const void* p, void* out, void* s) {
+  return agb_fem_eval(f, AGB_HESS_PROD, u, p, nullptr, nullptr, nullptr, out, nullptr, s);
+}
+int agb_fem_hess_quad(agb_fem* f, const void* u, const void* p, double* out, void* s) {
+  return agb_fem_eval(f, AGB_HESS_QUAD, u, p, nullptr, nullptr, nullptr, nullptr, out, s);
+}
+
+// ---------------------------------------------------------------------------
+// model
+// ---------------------------------------------------------------------------
+int agb_model_destroy(agb_model* m) {
+  if (!m) return AGB_OK;
+  for (int32_t* p : m->d_slot_of_tv) dfree(p);
+  for (void* p : {(void*)m->d_off, m->d_fixed, m->d_force, m->d_u, m->d_p, m->d_slots,
+                  (void*)m->d_partials, (void*)m->d_counter})
+    dfree(p);
+  delete m;
+  return AGB_OK;
+}
+
+int agb_model_create(agb_space* space, int precision, int32_t n_pot, agb_fem* const* pots,
+                     const uint8_t* fixed_mask, const double* fixed_values, int32_t n_force,
+                     const int32_t* force_index, const double* force, agb_model** out) {
+  AGB_REQUIRE(out, AGB_E_INVALID, "agb_model_create: out is null");
+  *out = nullptr;
+  AGB_REQUIRE(space && n_pot >= 0 && (n_pot == 0 || pots), AGB_E_INVALID,
+              "agb_model_create: need a space and a potential array");
+  AGB_REQUIRE(precision == AGB_F32 || precision == AGB_F64, AGB_E_INVALID,
+              "agb_model_create: unknown precision %d", precision);
+  const int prec = precision;
+  for (int k = 0; k < n_pot; ++k) {
+    AGB_REQUIRE(pots[k], AGB_E_INVALID, "agb_model_create: potential %d is null", k);
+    AGB_REQUIRE(pots[k]->space == space, AGB_E_INVALID,
+                "agb_model_create: potential %d is on another space", k);
+    AGB_REQUIRE(pots[k]->precision == prec, AGB_E_INVALID,
+                "agb_model_create: potentials mix precisions");
+  }
+  AGB_REQUIRE(n_force >= 0 && (n_force == 0 || (force_index && force)), AGB_E_INVALID,
+              "agb_model_create: force arrays");
+  const int np = space->n_points;
+  for (int k = 0; k < n_force; ++k)
+    AGB_REQUIRE(force_index[k] >= 0 && force_index[k] < np, AGB_E_MESH,
+                "agb_model_create: force index %d out of range", force_index[k]);
+
+  agb_model* m = new (std::nothrow) agb_model();
+  AGB_REQUIRE(m, AGB_E_INVALID, "agb_model_create: out of host memory");
+  m->space = space;
+  m->precision = prec;
+  m->fems.assign(pots, pots + n_pot);
+  std::vector<const TilePlan*> plans;
+  for (agb_fem* f : m->fems) plans.push_back(&f->plan);
+  build_slots(np, plans, &m->slots, &m->off);
+  m->n_slots = m->off[np];
+  m->mask_internal.assign(np, 0);
+  m->fixed_internal.assign(3 * (size_t)np, 0.0);
+  m->force_internal.assign(3 * (size_t)np, 0.0);
+  for (int u = 0; u < np; ++u) {
+    const int i = space->internal_of_user[u];
+    uint8_t bits = 0;
+    for (int c = 0; c < 3; ++c) {
+      if (fixed_mask && fixed_mask[3 * (size_t)u + c]) bits |= (uint8_t)(1u << c);
+      if (fixed_values && (bits >> c & 1u)) m->fixed_internal[3 * (size_t)i + c] = fixed_values[3 * (size_t)u + c];
+    }
+    m->mask_internal[i] = bits;
+  }
+  for (int k = 0; k < n_force; ++k) {
+    const int i = space->internal_of_user[force_index[k]];
+    for (int c = 0; c < 3; ++c) m->force_internal[3 * (size_t)i + c] += force[3 * (size_t)k + c];
+  }
+  m->n_force = n_force;
+  const size_t v4 = v4_bytes(prec);
+  int rc = dupload(&m->d_off, m->off);
+  m->d_slot_of_tv.assign(n_pot, nullptr);
+  for (int k = 0; k < n_pot && !rc; ++k) rc = dupload(&m->d_slot_of_tv[k], m->slots[k].slot_of_tv);
+  if (!rc) rc = dalloc_bytes(&m->d_fixed, v4 * np);
+  if (!rc) {
+    if (prec == AGB_F64) {
+      auto h = pack_v4<double>(m->fixed_internal, &m->mask_internal);
+      rc = upload(m->d_fixed, h.data(), v4 * np);
+    } else {
+      auto h = pack_v4<float>(m->fixed_internal, &m->mask_internal);
+      rc = upload(m->d_fixed, h.data(), v4 * np);
+    }
+  }
+  if (!rc && n_force > 0) {
+    rc = dalloc_bytes(&m->d_force, v4 * np);
+    if (!rc) {
+      if (prec == AGB_F64) {
+        auto h = pack_v4<double>(m->force_internal, nullptr);
+        rc = upload(m->d_force, h.data(), v4 * np);
+      } else {
+        auto h = pack_v4<float>(m->force_internal, nullptr);
+        rc = upload(m->d_force, h.data(), v4 * np);
+      }
+    }
+  }
+  int max_tiles = 0;
+  for (agb_fem* f : m->fems) max_tiles = std::max(max_tiles, f->plan.n_tiles);
+  const size_t n_part = (size_t)std::max(max_tiles, unpack_blocks(np)) * 2;
+  if (!rc) rc = dalloc_bytes(&m->d_u, v4 * np);
+  if (!rc) rc = dalloc_bytes(&m->d_p, v4 * np);
+  if (!rc) rc = dalloc_bytes(&m->d_slots, v4 * 3 * (size_t)m->n_slots);
+  if (!rc) rc = dalloc(&m->d_partials, n_part);
+  if (!rc) rc = dalloc(&m->d_counter, 1);
+  if (!rc && cudaMemset(m->d_counter, 0, sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
+  if (rc) {
+    agb_model_destroy(m);
+    return rc;
+  }
+  *out = m;
+  return AGB_OK;
+}
+
+int agb_model_eval(agb_model* m, unsigned flags, const void* u, const void* p, double* energy,
+                   void* grad, void* diag, void* prod, double* quad, void* stream) {
+  AGB_REQUIRE(m && u, AGB_E_INVALID, "agb_model_eval: null handle or u");
+  AGB_REQUIRE(!(flags & ~31u), AGB_E_INVALID, "agb_model_eval: unknown flags %u", flags);
+  const bool need_p = flags & (AGB_HESS_PROD | AGB_HESS_QUAD);
+  AGB_REQUIRE(!need_p || p, AGB_E_INVALID, "agb_model_eval: p is null");
+  AGB_REQUIRE(!(flags & AGB_FUN) || energy, AGB_E_INVALID, "agb_model_eval: energy is null");
+  AGB_REQUIRE(!(flags & AGB_GRAD) || grad, AGB_E_INVALID, "agb_model_eval: grad is null");
+  AGB_REQUIRE(!(flags & AGB_HESS_DIAG) || diag, AGB_E_INVALID, "agb_model_eval: hess_diag is null");
+  AGB_REQUIRE(!(flags & AGB_HESS_PROD) || prod, AGB_E_INVALID, "agb_model_eval: hess_prod is null");
+  AGB_REQUIRE(!(flags & AGB_HESS_QUAD) || quad, AGB_E_INVALID, "agb_model_eval: hess_quad is null");
+  cudaStream_t s = as_stream(stream);
+  const int np = m->space->n_points;
+  const size_t vec_bytes = 3 * (size_t)np * real_bytes(m->precision);
+  // WarpModel: zero, then every potential accumulates (warp/model/_model.py:13-36)
+  if (flags & AGB_FUN) AGB_CHECK_CUDA(cudaMemsetAsync(energy, 0, sizeof(double), s));
+  if (flags & AGB_HESS_QUAD) AGB_CHECK_CUDA(cudaMemsetAsync(quad, 0, sizeof(double), s));
+  if (flags & AGB_GRAD) AGB_CHECK_CUDA(cudaMemsetAsync(grad, 0, vec_bytes, s));
+  if (flags & AGB_HESS_DIAG) AGB_CHECK_CUDA(cudaMemsetAsync(diag, 0, vec_bytes, s));
+  if (flags & AGB_HESS_PROD) AGB_CHECK_CUDA(cudaMemsetAsync(prod, 0, vec_bytes, s));
+  if (!flags) return AGB_OK;
+  RC(check_launch(launch_pack(m->precision, np, m->space->d_user_of_internal, u, m->d_u,
+                              need_p ? p : nullptr, m->d_p, s),
+                  "pack"));
+  for (size_t k = 0; k < m->fems.size(); ++k)
+    RC(check_launch(launch_fem_eval(m->precision, m->fems[k]->view(), flags, m->d_u, m->d_p,
+                                    m->d_slot_of_tv[k], m->d_slots, m->n_slots, m->d_partials,
+                                    m->d_counter, energy, quad, s),
+                    "fem_eval"));
+  const unsigned vec = flags & (AGB_GRAD | AGB_HESS_DIAG | AGB_HESS_PROD | AGB_FUN);
+  const bool ext = m->d_force != nullptr;
+  if ((vec & ~AGB_FUN) || (ext && (flags & AGB_FUN)))
+    RC(check_launch(launch_unpack(m->precision, np, m->space->d_user_of_internal, m->d_off,
+                                  m->d_slots, m->n_slots, vec, grad, diag, prod, m->d_force,
+                                  m->d_u, m->d_partials, m->d_counter, energy, s),
+                    "unpack"));
+  return AGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// PNCG solver
+// ---------------------------------------------------------------------------
+void agb_pncg_default_params(agb_pncg_params* p) {
+  if (!p) return;
+  p->max_steps = 1500;
+  p->rtol = 1e-6;
+  p->atol = 0.0;
+  p->max_backtracking = 8;
+  p->armijo_c = 1e-4;
+  p->overstep = 1.0;
+  p->beta_max = 10.0;
+}
+
+int agb_solver_destroy(agb_solver* sv) {
+  if (!sv) return AGB_OK;
+  if (sv->loop_exec) cudaGraphExecDestroy(sv->loop_exec);
+  if (sv->step_exec) cudaGraphExecDestroy(sv->step_exec);
+  if (sv->capture_stream) cudaStreamDestroy(sv->capture_stream);
+  for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tv_vid,
+                  (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_x, sv->d_g, sv->d_d,
+                  sv->d_po, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
+                  sv->d_u_tmp})
+    dfree(p);
+  if (sv->h_state) cudaFreeHost(sv->h_state);
+  delete sv;
+  return AGB_OK;
+}
+
+int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** out) {
+  AGB_REQUIRE(out && m, AGB_E_INVALID, "agb_solver_create: null argument");
+  *out = nullptr;
+  AGB_REQUIRE(!m->fems.empty(), AGB_E_INVALID, "agb_solver_create: the model has no FEM potential");
+  const int mat = m->fems[0]->material;
+  for (agb_fem* f : m->fems)
+    AGB_REQUIRE(f->material == mat, AGB_E_INVALID,
+                "agb_solver_create: potentials of one solver must share a material");
+  agb_pncg_params prm;
+  agb_pncg_default_params(&prm);
+  if (params) prm = *params;
+  AGB_REQUIRE(prm.max_steps >= 0 && prm.max_backtracking >= 0 && prm.max_backtracking <= 60,
+              AGB_E_INVALID, "agb_solver_create: bad parameters");
+  agb_solver* sv = new (std::nothrow) agb_solver();
+  AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_create: out of host memory");
+  sv->model = m;
+  sv->params = prm;
+  sv->precision = m->precision;
+  const int np = m->space->n_points;
+  int rc = AGB_OK;
+  // element data: one potential is used in place; several are concatenated
+  std::vector<int32_t> slot_of_tv;
+  if (m->fems.size() == 1) {
+    sv->fv = m->fems[0]->view();
+    slot_of_tv = m->slots[0].slot_of_tv;
+  } else {
+    TilePlan& P = sv->plan;
+    P.tile_estart.assign(1, 0);
+    P.tile_vstart.assign(1, 0);
+    for (size_t k = 0; k < m->fems.size(); ++k) {
+      const TilePlan& Q = m->fems[k]->plan;
+      const int eoff = P.n_cells, voff = P.n_tv;
+      for (int t = 0; t < Q.n_tiles; ++t) {
+        P.tile_estart.push_back(eoff + Q.tile_estart[t + 1]);
+        P.tile_vstart.push_back(voff + Q.tile_vstart[t + 1]);
+      }
+      P.tv_vid.insert(P.tv_vid.end(), Q.tv_vid.begin(), Q.tv_vid.end());
+      P.ids.insert(P.ids.end(), Q.ids.begin(), Q.ids.end());
+      P.mudv.insert(P.mudv.end(), Q.mudv.begin(), Q.mudv.end());
+      P.lamdv.insert(P.lamdv.end(), Q.lamdv.begin(), Q.lamdv.end());
+      slot_of_tv.insert(slot_of_tv.end(), m->slots[k].slot_of_tv.begin(), m->slots[k].slot_of_tv.end());
+      P.n_cells += Q.n_cells;
+      P.n_tv += Q.n_tv;
+      P.n_tiles += Q.n_tiles;
+    }
+    P.D.assign(9 * (size_t)P.n_cells, 0.0);
+    int eoff = 0;
+    for (agb_fem* f : m->fems) {
+      const TilePlan& Q = f->plan;
+      for (int k = 0; k < 9; ++k)
+        std::memcpy(&P.D[(size_t)k * P.n_cells + eoff], &Q.D[(size_t)k * Q.n_cells],
+                    sizeof(double) * Q.n_cells);
+      eoff += Q.n_cells;
+    }
+    if (!rc) rc = dupload(&sv->d_tile_estart, P.tile_estart);
+    if (!rc) rc = dupload(&sv->d_tile_vstart, P.tile_vstart);
+    if (!rc) rc = dupload(&sv->d_tv_vid, P.tv_vid);
+    if (!rc) rc = upload_records(P, sv->precision, &sv->d_rec, &sv->d_ids);
+    sv->fv.material = mat;
+    sv->fv.n_tiles = P.n_tiles;
+    sv->fv.n_cells = P.n_cells;
+    sv->fv.tile_estart = sv->d_tile_estart;
+    sv->fv.tile_vstart = sv->d_tile_vstart;
+    sv->fv.tv_vid = sv->d_tv_vid;
+    sv->fv.rec = sv->d_rec;
+    sv->fv.ids = sv->d_ids;
+  }
+  if (!rc) rc = dupload(&sv->d_slot_of_tv, slot_of_tv);
+  const size_t v4 = v4_bytes(sv->precision);
+  const int vblocks = solver_vertex_blocks(np);
+  const size_t nt = (size_t)sv->fv.n_tiles;
+  const size_t n_part = nt * 6 + nt * 1 + (size_t)vblocks * 12 + nt * 3;
+  if (!rc) rc = dalloc_bytes(&sv->d_x, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_g, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_d, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_po, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_slots, v4 * 2 * (size_t)m->n_slots);
+  if (!rc) rc = dalloc_bytes(&sv->d_part, 8 * n_part);
+  if (!rc) rc = dalloc(&sv->d_cnt, 4);
+  if (!rc && cudaMemset(sv->d_cnt, 0, 4 * sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
+  if (!rc) rc = dalloc(&sv->d_state, 1);
+  if (!rc) rc = dalloc_bytes(&sv->d_u_tmp, 3 * real_bytes(sv->precision) * np);
+  if (!rc && cudaMallocHost((void**)&sv->h_state, sizeof(SolverState)) != cudaSuccess) rc = AGB_E_CUDA;
+  if (!rc && cudaStreamCreateWithFlags(&sv->capture_stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = AGB_E_CUDA;
+  if (!rc) {
+    SolverState st{};
+    st.rtol = prm.rtol;
+    st.atol = prm.atol;
+    st.armijo_c = prm.armijo_c;
+    st.overstep = prm.overstep;
+    st.beta_max = prm.beta_max;
+    st.max_steps = prm.max_steps;
+    st.max_bt = prm.max_backtracking;
+    st.done = 1;
+    st.result = AGB_RUNNING;
+    st.decided = 1;
+    rc = upload(sv->d_state, &st, sizeof(st));
+  }
+  if (rc) {
+    if (rc == AGB_E_CUDA && agb::last_error()[0] == 0) set_error("agb_solver_create: CUDA allocation failed");
+    agb_solver_destroy(sv);
+    return rc;
+  }
+  SolveArgs& a = sv->args;
+  a.fv = sv->fv;
+  a.n_points = np;
+  a.precision = sv->precision;
+  a.x = sv->d_x;
+  a.g = sv->d_g;
+  a.d = sv->d_d;
+  a.po = sv->d_po;
+  a.force = m->d_force;
+  a.slot_of_tv = sv->d_slot_of_tv;
+  a.off = m->d_off;
+  a.slots = sv->d_slots;
+  a.n_slots = m->n_slots;
+  a.st = sv->d_state;
+  char* part = (char*)sv->d_part;
+  a.part_a = part;
+  a.part_b = part + 8 * nt * 6;
+  a.part_v = part + 8 * (nt * 7);
+  a.part_t = part + 8 * (nt * 7 + (size_t)vblocks * 12);
+  a.cnt_a = sv->d_cnt;
+  a.cnt_v = sv->d_cnt + 1;
+  a.cnt_t = sv->d_cnt + 2;
+  a.vblocks = vblocks;
+  a.max_bt = prm.max_backtracking;
+  a.cond = 0;
+  *out = sv;
+  return AGB_OK;
+}
+
+int agb_solver_reset(agb_solver* sv, const void* u, void* stream) {
+  AGB_REQUIRE(sv && u, AGB_E_INVALID, "agb_solver_reset: null argument");
+  cudaStream_t s = as_stream(stream);
+  RC(check_launch(launch_solver_init(sv->args, u, sv->model->d_fixed,
+                                     sv->model->space->d_user_of_internal, s),
+                  "solver_init"));
+  RC(check_launch(launch_solver_first(sv->args, s), "solver_first"));
+  return AGB_OK;
+}
+
+static int build_loop_graph(agb_solver* sv) {
+  cudaGraph_t g = nullptr;
+  AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return check_launch(e, "cudaGraphConditionalHandleCreate");
+  }
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return check_launch(e, "cudaGraphAddNode(conditional)");
+  }
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(sv->capture_stream, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    SolveArgs a = sv->args;
+    a.cond = (unsigned long long)h;
+    cudaError_t le = launch_solver_iteration(a, true, sv->capture_stream);
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(sv->capture_stream, &captured);
+    if (e == cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->loop_exec, g, 0);
+  cudaGraphDestroy(g);
+  return check_launch(e, "solver loop graph");
+}
+
+static int build_step_graph(agb_solver* sv) {
+  cudaGraph_t g = nullptr;
+  AGB_CHECK_CUDA(cudaStreamBeginCapture(sv->capture_stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t le = launch_solver_iteration(sv->args, false, sv->capture_stream);
+  cudaError_t e = cudaStreamEndCapture(sv->capture_stream, &g);
+  if (e == cudaSuccess) e = le;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->step_exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  return check_launch(e, "solver step graph");
+}
+
+int agb_solver_iterate(agb_solver* sv, int32_t n_steps, void* stream) {
+  AGB_REQUIRE(sv && n_steps >= 0, AGB_E_INVALID, "agb_solver_iterate: bad argument");
+  if (n_steps == 0) return AGB_OK;
+  if (!sv->loop_exec) RC(build_loop_graph(sv));
+  cudaStream_t s = as_stream(stream);
+  RC(check_launch(launch_solver_set_limit(sv->args, n_steps, s), "set_limit"));
+  AGB_CHECK_CUDA(cudaGraphLaunch(sv->loop_exec, s));
+  return AGB_OK;
+}
+
+int agb_solver_step(agb_solver* sv, void* stream) {
+  AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_step: null handle");
+  if (!sv->step_exec) RC(build_step_graph(sv));
+  AGB_CHECK_CUDA(cudaGraphLaunch(sv->step_exec, as_stream(stream)));
+  return AGB_OK;
+}
+
+int agb_solver_read(agb_solver* sv, void* u_out, agb_pncg_stats* stats, void* stream) {
+  AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_read: null handle");
+  cudaStream_t s = as_stream(stream);
+  if (u_out)
+    RC(check_launch(launch_solver_unpack_x(sv->args, nullptr, sv->model->space->d_user_of_internal,
+                                           u_out, s),
+                    "unpack_x"));
+  AGB_CHECK_CUDA(cudaMemcpyAsync(sv->h_state, sv->d_state, sizeof(SolverState),
+                                 cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  const SolverState& st = *sv->h_state;
+  if (stats) {
+    stats->result = st.done ? st.result : AGB_RUNNING;
+    stats->n_steps = st.iter;
+    stats->grad_norm = st.gnorm;
+    stats->grad_norm_first = st.gnorm0;
+    stats->energy = st.energy;
+    stats->alpha = st.ls_ok ? st.t : 0.0;
+    stats->beta = st.beta;
+    stats->line_search_steps = st.ls_steps;
+    stats->line_search_ok = st.ls_ok;
+  }
+  AGB_REQUIRE(st.error == 0, AGB_E_DEVICE, "solver: device guard %d tripped", st.error);
+  return AGB_OK;
+}
+
+int agb_pncg_minimize_host(agb_solver* sv, void* u_host, agb_pncg_stats* stats, void* stream) {
+  AGB_REQUIRE(sv && u_host, AGB_E_INVALID, "agb_pncg_minimize_host: null argument");
+  cudaStream_t s = as_stream(stream);
+  const size_t bytes = 3 * real_bytes(sv->precision) * (size_t)sv->model->space->n_points;
+  AGB_CHECK_CUDA(cudaMemcpyAsync(sv->d_u_tmp, u_host, bytes, cudaMemcpyHostToDevice, s));
+  RC(agb_solver_reset(sv, sv->d_u_tmp, stream));
+  RC(agb_solver_iterate(sv, sv->params.max_steps, stream));
+  RC(agb_solver_read(sv, sv->d_u_tmp, stats, stream));
+  AGB_CHECK_CUDA(cudaMemcpyAsync(u_host, sv->d_u_tmp, bytes, cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  return AGB_OK;
+}
+
+}  // extern "C"

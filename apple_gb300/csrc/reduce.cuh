@@ -1,0 +1,168 @@
+// Global sums for the PNCG scalars (energy, p^T H p, dot products).
+//
+// GB300's FP64 rate is about 1/64 of its FP32 rate, so per-element FP64
+// adds would cost more than the memory pass they sit in.  Leaves therefore
+// accumulate in float-float form (hi + lo, error-free two-sum, about 44
+// significant bits), warps and blocks combine float-float pairs in a fixed
+// order, and each block writes one pair per quantity.  The last block to
+// finish (detected with a counter after a fence, no spinning) adds the block
+// partials in a fixed order and hands FP64 values to the scalar logic, so
+// every sum is deterministic for a given grid.  The FP64 build (R = double)
+// accumulates plain doubles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace agb {
+
+template <class R>
+struct Acc;
+
+template <>
+struct Acc<float> {
+  float hi, lo;  // no initialisers: usable in __shared__; value-initialise with {}
+  __device__ __forceinline__ void add(float b) {
+    const float s = hi + b;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (b - bb);
+    hi = s;
+    lo += err;
+  }
+  __device__ __forceinline__ void add(const Acc<float>& o) {
+    const float s = hi + o.hi;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (o.hi - bb);
+    hi = s;
+    lo = lo + o.lo + err;
+  }
+  __device__ __forceinline__ Acc<float> shfl_down(int off) const {
+    Acc<float> r{};
+    r.hi = __shfl_down_sync(0xffffffffu, hi, off);
+    r.lo = __shfl_down_sync(0xffffffffu, lo, off);
+    return r;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <>
+struct Acc<double> {
+  double v;
+  __device__ __forceinline__ void add(double b) { v += b; }
+  __device__ __forceinline__ void add(const Acc<double>& o) { v += o.v; }
+  __device__ __forceinline__ Acc<double> shfl_down(int off) const {
+    Acc<double> r{};
+    r.v = __shfl_down_sync(0xffffffffu, v, off);
+    return r;
+  }
+  __device__ __forceinline__ double value() const { return v; }
+};
+
+// Storage of one partial in global memory.
+template <class R>
+struct AccStore;
+template <>
+struct AccStore<float> {
+  float2 p;
+};
+template <>
+struct AccStore<double> {
+  double p;
+};
+
+template <class R>
+__device__ __forceinline__ AccStore<R> acc_store(const Acc<R>& a);
+template <>
+__device__ __forceinline__ AccStore<float> acc_store<float>(const Acc<float>& a) {
+  return AccStore<float>{make_float2(a.hi, a.lo)};
+}
+template <>
+__device__ __forceinline__ AccStore<double> acc_store<double>(const Acc<double>& a) {
+  return AccStore<double>{a.v};
+}
+
+template <class R>
+__device__ __forceinline__ Acc<R> acc_load(const AccStore<R>* s);
+template <>
+__device__ __forceinline__ Acc<float> acc_load<float>(const AccStore<float>* s) {
+  const float2 v = __ldcg(&s->p);
+  Acc<float> a{};
+  a.hi = v.x;
+  a.lo = v.y;
+  return a;
+}
+template <>
+__device__ __forceinline__ Acc<double> acc_load<double>(const AccStore<double>* s) {
+  Acc<double> a{};
+  a.v = __ldcg(&s->p);
+  return a;
+}
+
+// Block-wide reduction of N accumulators.  Result valid in thread 0.
+// `scratch` must hold (blockDim/32) * N entries.
+template <int N, class R>
+__device__ __forceinline__ void block_reduce(Acc<R> (&a)[N], Acc<R>* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) a[k].add(a[k].shfl_down(off));
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) scratch[warp * N + k] = a[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      Acc<R> s = scratch[k];
+      for (int w = 1; w < nw; ++w) s.add(scratch[w * N + k]);
+      a[k] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Write this block's N partials; return true in the last block to finish,
+// in which `total` (thread 0 only) holds the fixed-order sums over all
+// `nblocks` partials.  Resets the counter for the next launch.
+template <int N, class R>
+__device__ __forceinline__ bool grid_reduce(Acc<R> (&a)[N], AccStore<R>* partials, unsigned* counter,
+                                            int nblocks, Acc<R>* scratch, double (&total)[N]) {
+  __shared__ bool s_last;
+  block_reduce<N, R>(a, scratch);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) partials[(size_t)blockIdx.x * N + k] = acc_store(a[k]);
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    s_last = (prev == (unsigned)nblocks - 1u);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  Acc<R> b[N] = {};
+  for (int blk = threadIdx.x; blk < nblocks; blk += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) b[k].add(acc_load<R>(partials + (size_t)blk * N + k));
+  }
+  block_reduce<N, R>(b, scratch);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) total[k] = b[k].value();
+    *counter = 0u;
+  }
+  return true;
+}
+
+// Sum a range of stored partials inside one block (thread 0 gets the value).
+template <class R>
+__device__ __forceinline__ double block_sum_partials(const AccStore<R>* partials, int n, int stride,
+                                                     Acc<R>* scratch) {
+  Acc<R> b[1] = {};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) b[0].add(acc_load<R>(partials + (size_t)i * stride));
+  block_reduce<1, R>(b, scratch);
+  return b[0].value();
+}
+
+}  // namespace agb

@@ -1,0 +1,571 @@
+// PNCG on the device (benches/bench_pncg_branching_backends.py:254-456,
+// 606-679, with the first trial step alpha_0 = overstep * (-g.p / p.Hp)).
+//
+// One iteration k is three kernels, all driven by SolverState in device
+// memory (no host round trip):
+//   direction pass  p_k = -P_k g_k + beta_k p_{k-1} formed per tile vertex;
+//                   per element: clamped p^T H_e p (alpha_0) and, for stable
+//                   Neo-Hookean, the coefficients c_2..c_6 of
+//                   Psi_e(F + t dF) - Psi_e(F) - t P:dF, which is an exact
+//                   polynomial in t; the last block runs the Armijo
+//                   backtracking of the reference on
+//                   dE(t) = t g.p + sum_m C_m t^m -- the same trial points
+//                   and decisions as evaluating fun(x + t p) per trial,
+//                   without the O(1) cancellation of f(x+tp) - f(x)
+//   [ARAP]          trial passes evaluate the remainder at up to three trial
+//                   steps each (ARAP is not polynomial in t)
+//   gradient pass   at x_{k+1} = x_k + t p_k: energy, gradient, clamped
+//                   Hessian diagonal -> tile slots
+//   vertex pass     x_{k+1}, g_{k+1}, d_{k+1}, p_k written; dot products of
+//                   the Dai-Kou beta, the descent check and the convergence
+//                   norm reduced; the last block decides beta_{k+1}, the
+//                   preconditioner mean and termination, and sets the CUDA
+//                   graph's while-condition.
+#include <math.h>
+
+#include "kernels.h"
+#include "solver.h"
+#include "tile.cuh"
+
+namespace agb {
+
+constexpr int kVThreads = 256;
+
+int solver_vertex_blocks(int n_points) {
+  int b = (n_points + kVThreads - 1) / kVThreads;
+  return b < 1 ? 1 : (b > 1216 ? 1216 : b);
+}
+
+__device__ __forceinline__ double initial_alpha(double gd, double hq, double overstep) {
+  double a = -gd / hq;
+  if (isnan(a)) a = 0.0;
+  if (isinf(a)) a = a > 0 ? 1.0 : 0.0;
+  if (!(a > 0.0 && isfinite(a))) a = 1.0;
+  return a * overstep;
+}
+
+// A rejected line search restarts with steepest descent; along steepest
+// descent it ends the solve (LINE_SEARCH_FAILED).
+__device__ __forceinline__ void reject_step(SolverState* st, int ls) {
+  st->t = 0.0;
+  st->delta_e = 0.0;
+  st->ls_ok = 0;
+  st->ls_steps = ls;
+  st->reset_beta = 1;
+  if (st->beta == 0.0) st->ls_fail = 1;
+}
+
+template <class R>
+__device__ __forceinline__ void stage_direction(const SolveArgs& a, int vs, int nv, R beta,
+                                                R inv_mean, R t, bool want_p, R (*sx)[kTileVerts],
+                                                R (*sp)[kTileVerts]) {
+  const V4<R>* X = (const V4<R>*)a.x;
+  const V4<R>* G = (const V4<R>*)a.g;
+  const V4<R>* D = (const V4<R>*)a.d;
+  const V4<R>* PO = (const V4<R>*)a.po;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const int v = a.fv.tv_vid[vs + i];
+    const V4<R> x = ldg4(X + v), g = ldg4(G + v), d = ldg4(D + v), po = ldg4(PO + v);
+    R p[3];
+    pdir(g, d, po, beta, inv_mean, p);
+    sx[0][i] = fma_rn(t, p[0], x.x);
+    sx[1][i] = fma_rn(t, p[1], x.y);
+    sx[2][i] = fma_rn(t, p[2], x.z);
+    if (want_p) {
+      sp[0][i] = p[0];
+      sp[1][i] = p[1];
+      sp[2][i] = p[2];
+    }
+  }
+}
+
+template <class R>
+__device__ __forceinline__ void gather_corners(R (*s)[kTileVerts], const int (&l)[4], R (&w)[4][3]) {
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) w[a][c] = s[c][l[a]];
+}
+
+// ---------------------------------------------------------------------------
+// direction pass
+// ---------------------------------------------------------------------------
+template <class R, int MAT>
+__global__ void __launch_bounds__(kElemThreads) solver_dir_kernel(SolveArgs a, int use_cond) {
+  constexpr int N = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 6 : 1;
+  __shared__ R sx[3][kTileVerts];
+  __shared__ R sp[3][kTileVerts];
+  __shared__ Acc<R> red[(kElemThreads / 32) * N];
+  SolverState* st = a.st;
+  if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
+  if (st->done) return;
+  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
+  const int tile = blockIdx.x;
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sx, sp);
+  __syncthreads();
+
+  Acc<R> sums[N] = {};
+  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem<R>(a.fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R w[4][3], G[3][3], dF[3][3];
+    gather_corners(sx, l, w);
+    corner_gradient(w, geo.D, G);
+    gather_corners(sp, l, w);
+    corner_gradient(w, geo.D, dF);
+    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      SnhPoint<R> s;
+      snh_prepare(G, s);
+      SnhDir<R> d;
+      snh_dir(s, dF, d);
+      sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
+      R c[5];
+      snh_poly(s, d, geo.mu, geo.lam, c);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
+    } else {
+      const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
+      Svd<R> sv;
+      svd_rv(G, jm1, sv);
+      R lk[3];
+      arap_lambdas(sv, lk);
+      sums[0].add(fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0)));
+    }
+  }
+  double tot[N];
+  if (!grid_reduce<N, R>(sums, (AccStore<R>*)a.part_a, a.cnt_a, gridDim.x, red, tot)) return;
+  if (threadIdx.x != 0) return;
+  const double hq = tot[0];
+  st->hq = hq;
+  const double gd = st->gd;
+  const double a0 = initial_alpha(gd, hq, st->overstep);
+  st->alpha0 = a0;
+  if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+    double t = a0, de = 0.0;
+    int ls = 0;
+    bool ok = false;
+    for (;;) {
+      de = t * (gd + t * (tot[1] + t * (tot[2] + t * (tot[3] + t * (tot[4] + t * tot[5])))));
+      ok = isfinite(de) && de <= st->armijo_c * t * gd;
+      if (ok || ls >= st->max_bt || !(t > 0.0)) break;
+      t *= 0.5;
+      ++ls;
+    }
+    if (ok) {
+      st->t = t;
+      st->delta_e = de;
+      st->ls_ok = 1;
+      st->ls_steps = ls;
+    } else {
+      reject_step(st, ls);
+    }
+    st->decided = 1;
+  } else {
+    st->t = 0.0;
+    st->decided = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ARAP trial pass: remainders at trial steps alpha_0 2^-j, j = j0 .. j0+2
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a, int j0) {
+  __shared__ R sx[3][kTileVerts];
+  __shared__ R sp[3][kTileVerts];
+  __shared__ Acc<R> red[(kElemThreads / 32) * 3];
+  SolverState* st = a.st;
+  if (st->done || st->decided) return;
+  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
+  const double a0 = st->alpha0;
+  R tj[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) tj[j] = (R)ldexp(a0, -(j0 + j));
+  const int tile = blockIdx.x;
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sx, sp);
+  __syncthreads();
+  Acc<R> sums[3] = {};
+  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem<R>(a.fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R w[4][3], G[3][3], dF[3][3];
+    gather_corners(sx, l, w);
+    corner_gradient(w, geo.D, G);
+    gather_corners(sp, l, w);
+    corner_gradient(w, geo.D, dF);
+    Svd<R> base;
+    svd_rv(G, (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G), base);
+#pragma unroll 1
+    for (int j = 0; j < 3; ++j) {
+      R Gt[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Gt[i][k] = fma_rn(tj[j], dF[i][k], G[i][k]);
+      Svd<R> trial;
+      svd_rv(Gt, (Gt[0][0] + Gt[1][1] + Gt[2][2]) + inv2(Gt) + det3(Gt), trial);
+      sums[j].add(arap_remainder(base, trial, tj[j], dF, geo.mu));
+    }
+  }
+  double tot[3];
+  if (!grid_reduce<3, R>(sums, (AccStore<R>*)a.part_t, a.cnt_t, gridDim.x, red, tot)) return;
+  if (threadIdx.x != 0) return;
+  const double gd = st->gd;
+  for (int j = 0; j < 3; ++j) {
+    const int J = j0 + j;
+    if (J > st->max_bt) break;
+    const double t = ldexp(a0, -J);
+    const double de = gd * t + tot[j];
+    if (isfinite(de) && de <= st->armijo_c * t * gd) {
+      st->t = t;
+      st->delta_e = de;
+      st->ls_ok = 1;
+      st->ls_steps = J;
+      st->decided = 1;
+      return;
+    }
+  }
+  if (j0 + 2 >= st->max_bt) {
+    reject_step(st, st->max_bt);
+    st->decided = 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// gradient pass at x + t p
+// ---------------------------------------------------------------------------
+template <class R, int MAT>
+__global__ void __launch_bounds__(kElemThreads) solver_grad_kernel(SolveArgs a) {
+  __shared__ R sx[3][kTileVerts];
+  __shared__ R acc[6][kTileVerts];
+  __shared__ Acc<R> red[kElemThreads / 32];
+  SolverState* st = a.st;
+  if (st->done) return;
+  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean, t = (R)st->t;
+  const int tile = blockIdx.x;
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  stage_direction<R>(a, vs, nv, beta, inv_mean, t, false, sx, nullptr);
+  for (int i = threadIdx.x; i < nv; i += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q][i] = R(0);
+  __syncthreads();
+
+  Acc<R> sums[1] = {};
+  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem<R>(a.fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R w[4][3], G[3][3], P[3][3], f[4][3];
+    gather_corners(sx, l, w);
+    corner_gradient(w, geo.D, G);
+    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      SnhPoint<R> s;
+      snh_prepare(G, s);
+      sums[0].add(snh_energy(s, geo.mu, geo.lam));
+      snh_pk1(s, geo.mu, geo.lam, P);
+      corner_vjp(P, geo.D, f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) atomicAdd(&acc[c][l[k]], f[k][c]);
+      snh_hess_diag(s, geo.D, geo.mu, geo.lam, f);
+    } else {
+      const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
+      Svd<R> sv;
+      svd_rv(G, jm1, sv);
+      sums[0].add(arap_energy(sv, geo.mu));
+      arap_pk1(sv, geo.mu, P);
+      corner_vjp(P, geo.D, f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) atomicAdd(&acc[c][l[k]], f[k][c]);
+      R lk[3];
+      arap_lambdas(sv, lk);
+      arap_hess_diag(sv, lk, geo.D, geo.mu, f);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) atomicAdd(&acc[3 + c][l[k]], fmax(f[k][c], R(0)));
+  }
+  __syncthreads();
+  V4<R>* slots = (V4<R>*)a.slots;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const int s = a.slot_of_tv[vs + i];
+    slots[s] = V4<R>{acc[0][i], acc[1][i], acc[2][i], R(0)};
+    slots[(size_t)a.n_slots + s] = V4<R>{acc[3][i], acc[4][i], acc[5][i], R(0)};
+  }
+  block_reduce<1, R>(sums, red);
+  if (threadIdx.x == 0) ((AccStore<R>*)a.part_b)[blockIdx.x] = acc_store(sums[0]);
+}
+
+// ---------------------------------------------------------------------------
+// vertex pass
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, int use_cond) {
+  constexpr int N = 12;
+  __shared__ Acc<R> red[(kVThreads / 32) * N];
+  SolverState* st = a.st;
+  if (st->done) {
+    if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
+      cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
+    return;
+  }
+  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean, t = (R)st->t;
+  V4<R>* X = (V4<R>*)a.x;
+  V4<R>* Gv = (V4<R>*)a.g;
+  V4<R>* Dv = (V4<R>*)a.d;
+  V4<R>* PO = (V4<R>*)a.po;
+  const V4<R>* F = (const V4<R>*)a.force;
+  const V4<R>* slots = (const V4<R>*)a.slots;
+  // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
+  Acc<R> s[N] = {};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) {
+    const V4<R> x = X[i], g = Gv[i], d = Dv[i], po = PO[i];
+    const int mask = (int)x.w;
+    R p[3];
+    pdir(g, d, po, beta, inv_mean, p);
+    const R xn[3] = {fma_rn(t, p[0], x.x), fma_rn(t, p[1], x.y), fma_rn(t, p[2], x.z)};
+    R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
+    for (int k = a.off[i]; k < a.off[i + 1]; ++k) {
+      const V4<R> sg = slots[k], sd = slots[(size_t)a.n_slots + k];
+      gs[0] += sg.x;
+      gs[1] += sg.y;
+      gs[2] += sg.z;
+      ds[0] += sd.x;
+      ds[1] += sd.y;
+      ds[2] += sd.z;
+    }
+    if (F) {
+      const V4<R> f = ldg4(F + i);
+      gs[0] -= f.x;
+      gs[1] -= f.y;
+      gs[2] -= f.z;
+      s[11].add(-(f.x * xn[0] + f.y * xn[1] + f.z * xn[2]));
+    }
+    const R go[3] = {g.x, g.y, g.z};
+    R gn[3], dn[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const bool fixed = (mask >> c) & 1;
+      gn[c] = fixed ? R(0) : gs[c];
+      dn[c] = fixed ? R(0) : ds[c];
+      if (fixed) continue;
+      const R y = gn[c] - go[c];
+      const R ad = fabs(dn[c]);
+      if (ad > R(0)) {
+        const R P = rcp_rn(ad);
+        s[0].add(gn[c] * gn[c] * P);
+        s[1].add(gn[c] * y * P);
+        s[2].add(y * y * P);
+        s[3].add(ad);
+        s[4].add(R(1));
+      } else {
+        s[5].add(gn[c] * gn[c]);
+        s[6].add(gn[c] * y);
+        s[7].add(y * y);
+      }
+      s[8].add(y * p[c]);
+      s[9].add(p[c] * gn[c]);
+      s[10].add(gn[c] * gn[c]);
+    }
+    X[i] = V4<R>{xn[0], xn[1], xn[2], x.w};
+    Gv[i] = V4<R>{gn[0], gn[1], gn[2], R(0)};
+    Dv[i] = V4<R>{dn[0], dn[1], dn[2], R(0)};
+    PO[i] = V4<R>{p[0], p[1], p[2], R(0)};
+  }
+  double tot[N];
+  if (!grid_reduce<N, R>(s, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
+  const double elastic =
+      block_sum_partials<R>((const AccStore<R>*)a.part_b, a.fv.n_tiles, 1, red);
+  if (threadIdx.x != 0) return;
+  const double cnt = tot[4], sad = tot[3];
+  const double inv_m = (cnt > 0.0 && sad > 0.0) ? cnt / sad : 1.0;
+  const double gPg = tot[0] + inv_m * tot[5];
+  const double gPy = tot[1] + inv_m * tot[6];
+  const double yPy = tot[2] + inv_m * tot[7];
+  const double yp = tot[8], pg = tot[9], gg = tot[10];
+  const double gnorm = sqrt(gg);
+  const double energy = elastic + tot[11];
+  const bool first = st->init != 0;
+  double b = 0.0;
+  if (!first) {
+    b = fabs(yp) > 1.0e-12 ? gPy / yp - (yPy / yp) * (pg / yp) : INFINITY;
+    if (st->reset_beta || !isfinite(b) || fabs(b) > st->beta_max) b = 0.0;
+  }
+  double gd = -gPg + b * pg;
+  if (!(isfinite(gd) && gd < 0.0)) {
+    b = 0.0;
+    gd = -gPg;
+  }
+  st->beta = b;
+  st->inv_mean = inv_m;
+  st->gd = gd;
+  st->gnorm = gnorm;
+  st->energy = energy;
+  st->reset_beta = 0;
+  if (first) {
+    st->gnorm0 = gnorm;
+    st->init = 0;
+  } else {
+    st->iter += 1;
+  }
+  int result = AGB_RUNNING;
+  if (!isfinite(gnorm) || !isfinite(energy))
+    result = AGB_NAN_ENCOUNTERED;
+  else if (!first && st->ls_fail)
+    result = AGB_LINE_SEARCH_FAILED;
+  else if (gnorm <= fmax(st->atol, st->rtol * st->gnorm0))
+    result = AGB_PRIMARY_SUCCESS;
+  else if (st->iter >= st->max_steps)
+    result = AGB_MAX_STEPS_REACHED;
+  if (result != AGB_RUNNING) {
+    st->done = 1;
+    st->result = result;
+  }
+  if (use_cond)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
+                            (!st->done && st->iter < st->iter_limit) ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
+// set-up and read-back
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V4<R>* __restrict__ fixed,
+                                   const int32_t* __restrict__ uoi) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) {
+    const size_t k = 3 * (size_t)uoi[i];
+    const V4<R> fx = fixed[i];
+    const int mask = (int)fx.w;
+    V4<R> x{u[k], u[k + 1], u[k + 2], fx.w};
+    if (mask & 1) x.x = fx.x;
+    if (mask & 2) x.y = fx.y;
+    if (mask & 4) x.z = fx.z;
+    ((V4<R>*)a.x)[i] = x;
+    ((V4<R>*)a.g)[i] = V4<R>{R(0), R(0), R(0), R(0)};
+    ((V4<R>*)a.d)[i] = V4<R>{R(0), R(0), R(0), R(0)};
+    ((V4<R>*)a.po)[i] = V4<R>{R(0), R(0), R(0), R(0)};
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    SolverState* st = a.st;
+    st->beta = 0.0;
+    st->inv_mean = 1.0;
+    st->gd = 0.0;
+    st->t = 0.0;
+    st->alpha0 = 0.0;
+    st->hq = 0.0;
+    st->gnorm = 0.0;
+    st->gnorm0 = 0.0;
+    st->energy = 0.0;
+    st->delta_e = 0.0;
+    st->iter = 0;
+    st->iter_limit = 0;
+    st->done = 0;
+    st->result = AGB_RUNNING;
+    st->init = 1;
+    st->reset_beta = 0;
+    st->ls_fail = 0;
+    st->ls_steps = 0;
+    st->ls_ok = 0;
+    st->decided = 1;
+    st->error = 0;
+  }
+}
+
+__global__ void solver_set_limit_kernel(SolverState* st, int n) { st->iter_limit = st->iter + n; }
+
+template <class R>
+__global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ x, const int32_t* __restrict__ uoi,
+                                     R* __restrict__ u) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const size_t k = 3 * (size_t)uoi[i];
+    const V4<R> v = x[i];
+    u[k] = v.x;
+    u[k + 1] = v.y;
+    u[k + 2] = v.z;
+  }
+}
+
+cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,
+                               const int32_t* uoi, cudaStream_t s) {
+  const int blocks = solver_vertex_blocks(a.n_points);
+  if (a.precision == AGB_F64)
+    solver_init_kernel<double><<<blocks, kVThreads, 0, s>>>(a, (const double*)u_user,
+                                                           (const V4<double>*)fixed, uoi);
+  else
+    solver_init_kernel<float><<<blocks, kVThreads, 0, s>>>(a, (const float*)u_user,
+                                                          (const V4<float>*)fixed, uoi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solver_set_limit(const SolveArgs& a, int n_steps, cudaStream_t s) {
+  solver_set_limit_kernel<<<1, 1, 0, s>>>(a.st, n_steps);
+  return cudaGetLastError();
+}
+
+template <class R, int MAT>
+static void launch_iteration_t(const SolveArgs& a, bool use_cond, bool first, int max_bt,
+                               cudaStream_t s) {
+  const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
+  if (!first) {
+    solver_dir_kernel<R, MAT><<<eg, eb, 0, s>>>(a, use_cond ? 1 : 0);
+    if constexpr (MAT == AGB_ARAP) {
+      for (int j0 = 0; j0 <= max_bt; j0 += 3) solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0);
+    }
+  }
+  solver_grad_kernel<R, MAT><<<eg, eb, 0, s>>>(a);
+  solver_vertex_kernel<R><<<a.vblocks, kVThreads, 0, s>>>(a, use_cond ? 1 : 0);
+}
+
+static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool first, cudaStream_t s) {
+  const int max_bt = a.max_bt;
+  if (a.fv.n_tiles == 0) return cudaErrorInvalidValue;
+  if (a.precision == AGB_F64) {
+    if (a.fv.material == AGB_ARAP)
+      launch_iteration_t<double, AGB_ARAP>(a, use_cond, first, max_bt, s);
+    else
+      launch_iteration_t<double, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
+  } else {
+    if (a.fv.material == AGB_ARAP)
+      launch_iteration_t<float, AGB_ARAP>(a, use_cond, first, max_bt, s);
+    else
+      launch_iteration_t<float, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solver_iteration(const SolveArgs& a, bool use_cond, cudaStream_t s) {
+  return launch_iteration(a, use_cond, false, s);
+}
+
+cudaError_t launch_solver_first(const SolveArgs& a, cudaStream_t s) {
+  return launch_iteration(a, false, true, s);
+}
+
+cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_t* uoi, void* u,
+                                   cudaStream_t s) {
+  const int blocks = solver_vertex_blocks(a.n_points);
+  if (a.precision == AGB_F64)
+    solver_unpack_kernel<double><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<double>*)a.x, uoi,
+                                                             (double*)u);
+  else
+    solver_unpack_kernel<float><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<float>*)a.x, uoi,
+                                                            (float*)u);
+  return cudaGetLastError();
+}
+
+}  // namespace agb

@@ -1,0 +1,113 @@
+// Device-resident PNCG state and the solver handle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "agb_internal.h"
+
+namespace agb {
+
+// Scalars of the PNCG iteration, kept in device memory and updated only by
+// the last block of a pass (thread 0), so that an iteration runs without a
+// host round trip.  Layout is plain-old-data for cudaMemcpy.
+struct SolverState {
+  // current direction coefficients: p = -P g + beta p_prev, P from d and inv_mean
+  double beta;
+  double inv_mean;
+  double gd;        // g . p for the current p (<0 for a descent direction)
+  double t;         // accepted step of the current iteration (0 if rejected)
+  double alpha0;    // first trial step (ARAP trial passes)
+  double hq;        // clamped p^T H p
+  double gnorm;     // ||g|| over free DOFs at x
+  double gnorm0;
+  double energy;    // total energy at x
+  double delta_e;   // predicted energy change of the accepted step
+  // parameters
+  double rtol, atol, armijo_c, overstep, beta_max;
+  int32_t max_steps;
+  int32_t max_bt;
+  // iteration bookkeeping
+  int32_t iter;
+  int32_t iter_limit;
+  int32_t done;
+  int32_t result;
+  int32_t init;        // next vertex pass is the initial one (beta = 0, record ||g_0||)
+  int32_t reset_beta;  // the last line search was rejected: restart with steepest descent
+  int32_t ls_fail;     // rejected along steepest descent: terminate
+  int32_t ls_steps;
+  int32_t ls_ok;
+  int32_t decided;     // ARAP: a trial pass has decided the step
+  int32_t error;       // device-side status (nonzero = a guard tripped)
+};
+
+// Everything a solver kernel needs, by value.
+struct SolveArgs {
+  FemView fv;
+  int n_points;
+  int precision;
+  void* x;     // V4<R> n_points, w = fixed mask bits
+  void* g;     // V4<R> free gradient (fixed components 0)
+  void* d;     // V4<R> Hessian diagonal (fixed components 0)
+  void* po;    // V4<R> previous direction
+  const void* force;  // V4<R> external force per vertex or null
+  const int32_t* slot_of_tv;
+  const int32_t* off;  // CSR over slots (n_points + 1)
+  void* slots;         // V4<R> [2][n_slots]
+  int32_t n_slots;
+  SolverState* st;
+  void* part_a;        // direction-pass partials (n_tiles x 6)
+  void* part_b;        // gradient-pass partials (n_tiles x 1)
+  void* part_v;        // vertex-pass partials (vblocks x 12)
+  void* part_t;        // ARAP trial partials (n_tiles x 3)
+  unsigned* cnt_a;
+  unsigned* cnt_v;
+  unsigned* cnt_t;
+  int vblocks;
+  int max_bt;               // Armijo halvings (ARAP trial passes launched)
+  unsigned long long cond;  // cudaGraphConditionalHandle or 0
+};
+
+cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,
+                               const int32_t* user_of_internal, cudaStream_t s);
+cudaError_t launch_solver_set_limit(const SolveArgs& a, int n_steps, cudaStream_t s);
+// one PNCG iteration: direction pass, [ARAP trial passes], gradient pass, vertex pass
+cudaError_t launch_solver_iteration(const SolveArgs& a, bool use_cond, cudaStream_t s);
+// gradient + vertex pass at t = 0 (initial g_0, diag_0)
+cudaError_t launch_solver_first(const SolveArgs& a, cudaStream_t s);
+cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void* fixed_unused,
+                                   const int32_t* user_of_internal, void* u_user, cudaStream_t s);
+int solver_vertex_blocks(int n_points);
+
+}  // namespace agb
+
+struct agb_solver {
+  agb_model* model = nullptr;
+  agb_pncg_params params{};
+  int precision = 0;
+  agb::FemView fv{};
+  // combined element data of all potentials (same material)
+  agb::TilePlan plan;
+  int32_t* d_tile_estart = nullptr;
+  int32_t* d_tile_vstart = nullptr;
+  int32_t* d_tv_vid = nullptr;
+  int32_t* d_slot_of_tv = nullptr;
+  void* d_rec = nullptr;
+  uint32_t* d_ids = nullptr;
+  // vertex state
+  void* d_x = nullptr;
+  void* d_g = nullptr;
+  void* d_d = nullptr;
+  void* d_po = nullptr;
+  void* d_slots = nullptr;
+  void* d_part = nullptr;
+  unsigned* d_cnt = nullptr;
+  agb::SolverState* d_state = nullptr;
+  agb::SolverState* h_state = nullptr;  // pinned
+  void* d_u_tmp = nullptr;              // caller-order staging for host I/O
+  agb::SolveArgs args{};
+  // graphs
+  cudaGraphExec_t loop_exec = nullptr;
+  cudaGraphExec_t step_exec = nullptr;
+  cudaStream_t capture_stream = nullptr;
+};

@@ -1,0 +1,193 @@
+/*
+ * apple_gb300 -- C ABI of the GB300-native FEM elasticity / PNCG hot path.
+ *
+ * Drop-in boundary for the reference's per-energy surface
+ *   WarpPotential.{fun,grad,hess_diag,hess_prod,hess_quad}(u[, p], output)
+ *     -- liblaf/apple src/liblaf/apple/warp/model/_potential.py:9-32,
+ *        implemented per material by warp/fem/_base.py:151-194 --
+ * the zero-then-accumulate model sum (warp/model/_model.py:13-36), the DOF
+ * map (forward/dof_map/_dof_map.py:30-49), the external force
+ * (warp/potential/_ext_force.py:17-90) and the PNCG solve entry
+ * (forward/_forward.py:52-56, Optimizer.minimize).
+ *
+ * Conventions
+ *  - Every entry point returns an int status: AGB_OK (0) or a negative
+ *    AGB_E_* code; agb_last_error() gives a message for the calling thread.
+ *  - Vector arguments are (n_points, 3) row-major arrays in the caller's
+ *    vertex order, of the potential's precision (float for AGB_F32 handles,
+ *    double for AGB_F64), in DEVICE memory unless a function says "host".
+ *    Scalar outputs (energy, p^T H p) are device doubles.
+ *  - Outputs are ACCUMULATED into (never zeroed), as in the reference.
+ *  - `stream` is a cudaStream_t passed as void*; NULL is the legacy stream.
+ *  - No torch or other library types cross this boundary.
+ */
+#ifndef APPLE_GB300_H
+#define APPLE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AGB_OK 0
+#define AGB_E_INVALID (-1)    /* bad argument (null pointer, size, enum) */
+#define AGB_E_CUDA (-2)       /* a CUDA runtime call failed */
+#define AGB_E_MESH (-3)       /* mesh rejected (index out of range, dV <= 0 where checked) */
+#define AGB_E_STATE (-4)      /* call not valid in the object's state */
+#define AGB_E_DEVICE (-5)     /* a kernel reported a device-side error status */
+
+/* precision of element arithmetic and vector storage */
+#define AGB_F32 0
+#define AGB_F64 1
+
+/* materials: warp/fem/_arap.py, warp/fem/_stable_neo_hookean.py */
+#define AGB_ARAP 0
+#define AGB_STABLE_NEO_HOOKEAN 1
+
+/* flags of agb_fem_eval */
+#define AGB_FUN 1u
+#define AGB_GRAD 2u
+#define AGB_HESS_DIAG 4u
+#define AGB_HESS_PROD 8u
+#define AGB_HESS_QUAD 16u
+
+typedef struct agb_space agb_space;
+typedef struct agb_fem agb_fem;
+typedef struct agb_model agb_model;
+typedef struct agb_solver agb_solver;
+
+const char* agb_last_error(void);
+const char* agb_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Vertex space: the global point set (ModelBuilder.add_vertices,
+ * forward/dof_map/_builder.py:41-50).  `points` (host, n_points x 3) fixes
+ * the device vertex order (Morton order of the rest positions); NULL keeps
+ * the caller's order.
+ * ------------------------------------------------------------------------- */
+int agb_space_create(int32_t n_points, const double* points, agb_space** out);
+int agb_space_destroy(agb_space* space);
+/* internal position of each caller vertex (host out, n_points int32) */
+int agb_space_order(const agb_space* space, int32_t* internal_of_user);
+
+/* Region.compute_grad (jax/fem/region/_region.py:84-108) on host arrays:
+ * dhdX (n_cells x 4 x 3, row a = grad of shape function a) and
+ * dV (n_cells) = det(Dm) / 6 * fraction (fraction may be NULL).  Returns
+ * AGB_OK; *n_nonpositive (may be NULL) counts cells with dV <= 0, which the
+ * reference only warns about (region/_region.py:98-99). */
+int agb_region_compute(int32_t n_cells, const int32_t* cells, int32_t n_points,
+                       const double* points, const double* fraction, double* dhdX, double* dV,
+                       int32_t* n_nonpositive);
+
+/* ---------------------------------------------------------------------------
+ * FEM potential over tetrahedra (WarpPotentialFem.from_region,
+ * warp/fem/_base.py:78-111).  All inputs are HOST arrays, copied.
+ *   cells     n_cells x 4, global point ids (GlobalPointId-mapped)
+ *   points    n_points x 3 rest positions; used when dhdX/dV are NULL to
+ *             compute them (jax/fem/region/_region.py:84-108)
+ *   dhdX      n_cells x 4 x 3 shape-function gradients, or NULL
+ *   dV        n_cells, or NULL (det(Dm)/6)
+ *   fraction  n_cells volume fraction scaling dV (utils/_material.py:19-23), or NULL
+ *   mu        n_cells Lame mu (cell data "mu")
+ *   lambda    n_cells Lame lambda (cell data "lambda"); ignored for ARAP
+ * Options: tile_elems (max elements per tile, 0 = default 1024).
+ * ------------------------------------------------------------------------- */
+int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cells,
+                   const int32_t* cells, const double* points, const double* dhdX,
+                   const double* dV, const double* fraction, const double* mu,
+                   const double* lambda, int32_t tile_elems, agb_fem** out);
+int agb_fem_destroy(agb_fem* fem);
+/* tile statistics: n_tiles, n_tile_vertices (host out; any may be NULL) */
+int agb_fem_info(const agb_fem* fem, int32_t* n_tiles, int32_t* n_tile_vertices);
+
+/* WarpPotential methods (warp/fem/_base.py:151-194); accumulate into output.
+ *   fun:       output[0] += sum_e Psi_e dV_e                       (_base.py:243-263)
+ *   grad:      output    += element gradients scattered            (_base.py:265-291)
+ *   hess_diag: output    += max(dV diag(H_e), 0) scattered         (_base.py:293-324)
+ *   hess_prod: output    += dV H_e p_e scattered                   (_base.py:326-351)
+ *   hess_quad: output[0] += sum_e max(dV p_e^T H_e p_e, 0)         (_base.py:353-383)
+ * ARAP hess_prod implements the intended H p (the reference's
+ * _arap.py:55-56 passes the operands of h4_prod/h5_prod in swapped order). */
+int agb_fem_fun(agb_fem* fem, const void* u, double* output, void* stream);
+int agb_fem_grad(agb_fem* fem, const void* u, void* output, void* stream);
+int agb_fem_hess_diag(agb_fem* fem, const void* u, void* output, void* stream);
+int agb_fem_hess_prod(agb_fem* fem, const void* u, const void* p, void* output, void* stream);
+int agb_fem_hess_quad(agb_fem* fem, const void* u, const void* p, double* output, void* stream);
+/* fused: any subset of AGB_* flags in one pass over the mesh; NULL outputs
+ * for unset flags.  p is needed for HESS_PROD and HESS_QUAD. */
+int agb_fem_eval(agb_fem* fem, unsigned flags, const void* u, const void* p, double* energy,
+                 void* grad, void* hess_diag, void* hess_prod, double* hess_quad, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Model = potentials + fixed DOFs + external force over one space
+ * (ModelBuilder.finalize, forward/_builder.py:27-40).  Host inputs, copied.
+ *   fixed_mask    n_points x 3 (nonzero = fixed component), or NULL
+ *   fixed_values  n_points x 3 displacement of fixed components, or NULL
+ *   force_index / force  n_force point ids and forces (ExternalForce), or 0/NULL
+ * The potentials (n_potentials >= 0) must share `space` and `precision`; they
+ * stay owned by the caller and must outlive the model.
+ * ------------------------------------------------------------------------- */
+int agb_model_create(agb_space* space, int precision, int32_t n_potentials, agb_fem* const* potentials,
+                     const uint8_t* fixed_mask, const double* fixed_values, int32_t n_force,
+                     const int32_t* force_index, const double* force, agb_model** out);
+int agb_model_destroy(agb_model* model);
+/* WarpModel.*: zero then accumulate all potentials and the external force
+ * (warp/model/_model.py:13-36, potential/_ext_force.py:17-39). */
+int agb_model_eval(agb_model* model, unsigned flags, const void* u, const void* p, double* energy,
+                   void* grad, void* hess_diag, void* hess_prod, double* hess_quad, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * PNCG (liblaf-peach PNCG as used by forward/_forward.py:22-30; iteration as
+ * benches/bench_pncg_branching_backends.py:254-456,606-679).
+ * ------------------------------------------------------------------------- */
+typedef struct agb_pncg_params {
+  int32_t max_steps;           /* ConvergenceCriteria.max_steps (default 1500) */
+  double rtol;                 /* converged: ||g|| <= max(atol, rtol ||g_0||) */
+  double atol;
+  int32_t max_backtracking;    /* Armijo halvings after the first trial (8) */
+  double armijo_c;             /* 1e-4 */
+  double overstep;             /* alpha_0 = overstep * (-g.p / p.Hp); 1 */
+  double beta_max;             /* |beta| above this resets to steepest descent (10) */
+} agb_pncg_params;
+
+#define AGB_PRIMARY_SUCCESS 0
+#define AGB_MAX_STEPS_REACHED 1
+#define AGB_LINE_SEARCH_FAILED 2
+#define AGB_NAN_ENCOUNTERED 3
+#define AGB_RUNNING 4
+
+typedef struct agb_pncg_stats {
+  int32_t result;              /* AGB_PRIMARY_SUCCESS ... AGB_RUNNING */
+  int32_t n_steps;
+  double grad_norm;            /* ||g|| over free DOFs at the returned u */
+  double grad_norm_first;
+  double energy;               /* total energy at the returned u */
+  double alpha;                /* last accepted step length (0 if rejected) */
+  double beta;                 /* last beta */
+  int32_t line_search_steps;   /* halvings in the last line search */
+  int32_t line_search_ok;
+} agb_pncg_stats;
+
+void agb_pncg_default_params(agb_pncg_params* params);
+
+int agb_solver_create(agb_model* model, const agb_pncg_params* params, agb_solver** out);
+int agb_solver_destroy(agb_solver* solver);
+/* load u (device, full vector; fixed components are overwritten by the
+ * model's fixed values) and evaluate g_0, hess_diag_0. */
+int agb_solver_reset(agb_solver* solver, const void* u, void* stream);
+/* run up to n_steps iterations (fewer if the solve terminates); the loop
+ * runs on the device as one CUDA graph launch (conditional while node). */
+int agb_solver_iterate(agb_solver* solver, int32_t n_steps, void* stream);
+/* exactly one iteration as a plain graph (benchmark building block) */
+int agb_solver_step(agb_solver* solver, void* stream);
+/* copy u out (device, caller order) and the stats (host); synchronises stream */
+int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
+/* Optimizer.minimize(problem, state, free) with HOST buffers: copies u_host
+ * in, solves to termination, copies the result back into u_host. */
+int agb_pncg_minimize_host(agb_solver* solver, void* u_host, agb_pncg_stats* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* APPLE_GB300_H */
