@@ -519,7 +519,7 @@ int agb_solver_destroy(agb_solver* sv) {
   if (sv->step_exec) cudaGraphExecDestroy(sv->step_exec);
   if (sv->capture_stream) cudaStreamDestroy(sv->capture_stream);
   for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tv_vid,
-                  (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_x, sv->d_g, sv->d_d,
+                  (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_x, sv->d_xlo, sv->d_g, sv->d_d,
                   sv->d_po, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
                   sv->d_u_tmp})
     dfree(p);
@@ -601,6 +601,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   const size_t nt = (size_t)sv->fv.n_tiles;
   const size_t n_part = nt * 6 + nt * 1 + (size_t)vblocks * 12 + nt * 3;
   if (!rc) rc = dalloc_bytes(&sv->d_x, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_xlo, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_g, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_d, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_po, v4 * np);
@@ -637,6 +638,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.n_points = np;
   a.precision = sv->precision;
   a.x = sv->d_x;
+  a.xlo = sv->d_xlo;
   a.g = sv->d_g;
   a.d = sv->d_d;
   a.po = sv->d_po;
@@ -759,6 +761,34 @@ int agb_solver_read(agb_solver* sv, void* u_out, agb_pncg_stats* stats, void* st
   }
   AGB_REQUIRE(st.error == 0, AGB_E_DEVICE, "solver: device guard %d tripped", st.error);
   return AGB_OK;
+}
+
+int agb_solver_time_passes(agb_solver* sv, int32_t reps, void* flush, size_t flush_bytes,
+                           float* ms, void* stream) {
+  AGB_REQUIRE(sv && ms && reps > 0, AGB_E_INVALID, "agb_solver_time_passes: bad argument");
+  cudaStream_t s = as_stream(stream);
+  cudaEvent_t e0, e1;
+  AGB_CHECK_CUDA(cudaEventCreate(&e0));
+  AGB_CHECK_CUDA(cudaEventCreate(&e1));
+  int rc = AGB_OK;
+  for (int which = 0; which < 3 && !rc; ++which) {
+    float total = 0.0f;
+    for (int r = 0; r < reps && !rc; ++r) {
+      if (flush && flush_bytes && cudaMemsetAsync(flush, r & 0xff, flush_bytes, s) != cudaSuccess) rc = AGB_E_CUDA;
+      if (!rc && cudaEventRecord(e0, s) != cudaSuccess) rc = AGB_E_CUDA;
+      if (!rc) rc = check_launch(launch_solver_pass(sv->args, which, s), "time_passes");
+      if (!rc && cudaEventRecord(e1, s) != cudaSuccess) rc = AGB_E_CUDA;
+      float t = 0.0f;
+      if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+        rc = AGB_E_CUDA;
+      total += t;
+    }
+    ms[which] = total / (float)reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == AGB_E_CUDA && agb::last_error()[0] == 0) set_error("agb_solver_time_passes: CUDA call failed");
+  return rc;
 }
 
 int agb_pncg_minimize_host(agb_solver* sv, void* u_host, agb_pncg_stats* stats, void* stream) {

@@ -57,20 +57,29 @@ __device__ __forceinline__ void reject_step(SolverState* st, int ls) {
 
 template <class R>
 __device__ __forceinline__ void stage_direction(const SolveArgs& a, int vs, int nv, R beta,
-                                                R inv_mean, R t, bool want_p, R (*sx)[kTileVerts],
-                                                R (*sp)[kTileVerts]) {
+                                                R inv_mean, R t, bool want_p, R (*sh)[kTileVerts],
+                                                R (*sl)[kTileVerts], R (*sp)[kTileVerts]) {
   const V4<R>* X = (const V4<R>*)a.x;
+  const V4<R>* XL = (const V4<R>*)a.xlo;
   const V4<R>* G = (const V4<R>*)a.g;
   const V4<R>* D = (const V4<R>*)a.d;
   const V4<R>* PO = (const V4<R>*)a.po;
   for (int i = threadIdx.x; i < nv; i += blockDim.x) {
     const int v = a.fv.tv_vid[vs + i];
-    const V4<R> x = ldg4(X + v), g = ldg4(G + v), d = ldg4(D + v), po = ldg4(PO + v);
+    const V4<R> x = ldg4(X + v), xl = ldg4(XL + v), g = ldg4(G + v), d = ldg4(D + v),
+                po = ldg4(PO + v);
     R p[3];
     pdir(g, d, po, beta, inv_mean, p);
-    sx[0][i] = fma_rn(t, p[0], x.x);
-    sx[1][i] = fma_rn(t, p[1], x.y);
-    sx[2][i] = fma_rn(t, p[2], x.z);
+    R hx = x.x, lx = xl.x, hy = x.y, ly = xl.y, hz = x.z, lz = xl.z;
+    pair_add(hx, lx, mul_rn(t, p[0]));
+    pair_add(hy, ly, mul_rn(t, p[1]));
+    pair_add(hz, lz, mul_rn(t, p[2]));
+    sh[0][i] = hx;
+    sh[1][i] = hy;
+    sh[2][i] = hz;
+    sl[0][i] = lx;
+    sl[1][i] = ly;
+    sl[2][i] = lz;
     if (want_p) {
       sp[0][i] = p[0];
       sp[1][i] = p[1];
@@ -87,13 +96,30 @@ __device__ __forceinline__ void gather_corners(R (*s)[kTileVerts], const int (&l
     for (int c = 0; c < 3; ++c) w[a][c] = s[c][l[a]];
 }
 
+// G = sum_a (x_a - x_0) D_a^T with the differences taken on hi + lo pairs
+template <class R>
+__device__ __forceinline__ void position_gradient(R (*sh)[kTileVerts], R (*sl)[kTileVerts],
+                                                  const int (&l)[4], const R (&D)[3][3],
+                                                  R (&G)[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const R h0 = sh[i][l[0]], l0 = sl[i][l[0]];
+    const R e1 = pair_diff(sh[i][l[1]], sl[i][l[1]], h0, l0);
+    const R e2 = pair_diff(sh[i][l[2]], sl[i][l[2]], h0, l0);
+    const R e3 = pair_diff(sh[i][l[3]], sl[i][l[3]], h0, l0);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) G[i][j] = e1 * D[0][j] + e2 * D[1][j] + e3 * D[2][j];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // direction pass
 // ---------------------------------------------------------------------------
 template <class R, int MAT>
 __global__ void __launch_bounds__(kElemThreads) solver_dir_kernel(SolveArgs a, int use_cond) {
   constexpr int N = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 6 : 1;
-  __shared__ R sx[3][kTileVerts];
+  __shared__ R sh[3][kTileVerts];
+  __shared__ R sl[3][kTileVerts];
   __shared__ R sp[3][kTileVerts];
   __shared__ Acc<R> red[(kElemThreads / 32) * N];
   SolverState* st = a.st;
@@ -104,7 +130,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_dir_kernel(SolveArgs a, i
   const int tile = blockIdx.x;
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
-  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sx, sp);
+  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sh, sl, sp);
   __syncthreads();
 
   Acc<R> sums[N] = {};
@@ -114,8 +140,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_dir_kernel(SolveArgs a, i
     load_elem<R>(a.fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R w[4][3], G[3][3], dF[3][3];
-    gather_corners(sx, l, w);
-    corner_gradient(w, geo.D, G);
+    position_gradient(sh, sl, l, geo.D, G);
     gather_corners(sp, l, w);
     corner_gradient(w, geo.D, dF);
     if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
@@ -176,7 +201,8 @@ __global__ void __launch_bounds__(kElemThreads) solver_dir_kernel(SolveArgs a, i
 // ---------------------------------------------------------------------------
 template <class R>
 __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a, int j0) {
-  __shared__ R sx[3][kTileVerts];
+  __shared__ R sh[3][kTileVerts];
+  __shared__ R sl[3][kTileVerts];
   __shared__ R sp[3][kTileVerts];
   __shared__ Acc<R> red[(kElemThreads / 32) * 3];
   SolverState* st = a.st;
@@ -189,7 +215,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
   const int tile = blockIdx.x;
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
-  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sx, sp);
+  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sh, sl, sp);
   __syncthreads();
   Acc<R> sums[3] = {};
   for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
@@ -198,8 +224,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
     load_elem<R>(a.fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R w[4][3], G[3][3], dF[3][3];
-    gather_corners(sx, l, w);
-    corner_gradient(w, geo.D, G);
+    position_gradient(sh, sl, l, geo.D, G);
     gather_corners(sp, l, w);
     corner_gradient(w, geo.D, dF);
     Svd<R> base;
@@ -245,7 +270,8 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
 // ---------------------------------------------------------------------------
 template <class R, int MAT>
 __global__ void __launch_bounds__(kElemThreads) solver_grad_kernel(SolveArgs a) {
-  __shared__ R sx[3][kTileVerts];
+  __shared__ R sh[3][kTileVerts];
+  __shared__ R sl[3][kTileVerts];
   __shared__ R acc[6][kTileVerts];
   __shared__ Acc<R> red[kElemThreads / 32];
   SolverState* st = a.st;
@@ -254,7 +280,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_grad_kernel(SolveArgs a) 
   const int tile = blockIdx.x;
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
-  stage_direction<R>(a, vs, nv, beta, inv_mean, t, false, sx, nullptr);
+  stage_direction<R>(a, vs, nv, beta, inv_mean, t, false, sh, sl, nullptr);
   for (int i = threadIdx.x; i < nv; i += blockDim.x)
 #pragma unroll
     for (int q = 0; q < 6; ++q) acc[q][i] = R(0);
@@ -266,9 +292,8 @@ __global__ void __launch_bounds__(kElemThreads) solver_grad_kernel(SolveArgs a) 
     uint32_t ids;
     load_elem<R>(a.fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
-    R w[4][3], G[3][3], P[3][3], f[4][3];
-    gather_corners(sx, l, w);
-    corner_gradient(w, geo.D, G);
+    R G[3][3], P[3][3], f[4][3];
+    position_gradient(sh, sl, l, geo.D, G);
     if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
       SnhPoint<R> s;
       snh_prepare(G, s);
@@ -326,6 +351,7 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   }
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean, t = (R)st->t;
   V4<R>* X = (V4<R>*)a.x;
+  V4<R>* XL = (V4<R>*)a.xlo;
   V4<R>* Gv = (V4<R>*)a.g;
   V4<R>* Dv = (V4<R>*)a.d;
   V4<R>* PO = (V4<R>*)a.po;
@@ -334,11 +360,14 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
   Acc<R> s[N] = {};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) {
-    const V4<R> x = X[i], g = Gv[i], d = Dv[i], po = PO[i];
+    const V4<R> x = X[i], xl = XL[i], g = Gv[i], d = Dv[i], po = PO[i];
     const int mask = (int)x.w;
     R p[3];
     pdir(g, d, po, beta, inv_mean, p);
-    const R xn[3] = {fma_rn(t, p[0], x.x), fma_rn(t, p[1], x.y), fma_rn(t, p[2], x.z)};
+    R xh[3] = {x.x, x.y, x.z}, xlo[3] = {xl.x, xl.y, xl.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) pair_add(xh[c], xlo[c], mul_rn(t, p[c]));
+    const R xn[3] = {xh[0] + xlo[0], xh[1] + xlo[1], xh[2] + xlo[2]};
     R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
     for (int k = a.off[i]; k < a.off[i + 1]; ++k) {
       const V4<R> sg = slots[k], sd = slots[(size_t)a.n_slots + k];
@@ -382,7 +411,8 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
       s[9].add(p[c] * gn[c]);
       s[10].add(gn[c] * gn[c]);
     }
-    X[i] = V4<R>{xn[0], xn[1], xn[2], x.w};
+    X[i] = V4<R>{xh[0], xh[1], xh[2], x.w};
+    XL[i] = V4<R>{xlo[0], xlo[1], xlo[2], R(0)};
     Gv[i] = V4<R>{gn[0], gn[1], gn[2], R(0)};
     Dv[i] = V4<R>{dn[0], dn[1], dn[2], R(0)};
     PO[i] = V4<R>{p[0], p[1], p[2], R(0)};
@@ -456,6 +486,7 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     if (mask & 2) x.y = fx.y;
     if (mask & 4) x.z = fx.z;
     ((V4<R>*)a.x)[i] = x;
+    ((V4<R>*)a.xlo)[i] = V4<R>{R(0), R(0), R(0), R(0)};
     ((V4<R>*)a.g)[i] = V4<R>{R(0), R(0), R(0), R(0)};
     ((V4<R>*)a.d)[i] = V4<R>{R(0), R(0), R(0), R(0)};
     ((V4<R>*)a.po)[i] = V4<R>{R(0), R(0), R(0), R(0)};
@@ -489,14 +520,14 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
 __global__ void solver_set_limit_kernel(SolverState* st, int n) { st->iter_limit = st->iter + n; }
 
 template <class R>
-__global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ x, const int32_t* __restrict__ uoi,
-                                     R* __restrict__ u) {
+__global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ x, const V4<R>* __restrict__ xlo,
+                                     const int32_t* __restrict__ uoi, R* __restrict__ u) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const size_t k = 3 * (size_t)uoi[i];
-    const V4<R> v = x[i];
-    u[k] = v.x;
-    u[k + 1] = v.y;
-    u[k + 2] = v.z;
+    const V4<R> v = x[i], l = xlo[i];
+    u[k] = v.x + l.x;
+    u[k + 1] = v.y + l.y;
+    u[k + 2] = v.z + l.z;
   }
 }
 
@@ -548,6 +579,29 @@ static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool firs
   return cudaGetLastError();
 }
 
+template <class R, int MAT>
+static void launch_pass_t(const SolveArgs& a, int which, cudaStream_t s) {
+  const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
+  if (which == 0) solver_dir_kernel<R, MAT><<<eg, eb, 0, s>>>(a, 0);
+  if (which == 1) solver_grad_kernel<R, MAT><<<eg, eb, 0, s>>>(a);
+  if (which == 2) solver_vertex_kernel<R><<<a.vblocks, kVThreads, 0, s>>>(a, 0);
+}
+
+cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s) {
+  if (a.precision == AGB_F64) {
+    if (a.fv.material == AGB_ARAP)
+      launch_pass_t<double, AGB_ARAP>(a, which, s);
+    else
+      launch_pass_t<double, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
+  } else {
+    if (a.fv.material == AGB_ARAP)
+      launch_pass_t<float, AGB_ARAP>(a, which, s);
+    else
+      launch_pass_t<float, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_solver_iteration(const SolveArgs& a, bool use_cond, cudaStream_t s) {
   return launch_iteration(a, use_cond, false, s);
 }
@@ -560,11 +614,11 @@ cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_
                                    cudaStream_t s) {
   const int blocks = solver_vertex_blocks(a.n_points);
   if (a.precision == AGB_F64)
-    solver_unpack_kernel<double><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<double>*)a.x, uoi,
-                                                             (double*)u);
+    solver_unpack_kernel<double><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<double>*)a.x,
+                                                             (const V4<double>*)a.xlo, uoi, (double*)u);
   else
-    solver_unpack_kernel<float><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<float>*)a.x, uoi,
-                                                            (float*)u);
+    solver_unpack_kernel<float><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<float>*)a.x,
+                                                            (const V4<float>*)a.xlo, uoi, (float*)u);
   return cudaGetLastError();
 }
 

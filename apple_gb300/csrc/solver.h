@@ -46,7 +46,8 @@ struct SolveArgs {
   FemView fv;
   int n_points;
   int precision;
-  void* x;     // V4<R> n_points, w = fixed mask bits
+  void* x;     // V4<R> n_points: position hi part, w = fixed mask bits
+  void* xlo;   // V4<R> n_points: position lo part (x = hi + lo)
   void* g;     // V4<R> free gradient (fixed components 0)
   void* d;     // V4<R> Hessian diagonal (fixed components 0)
   void* po;    // V4<R> previous direction
@@ -78,6 +79,8 @@ cudaError_t launch_solver_first(const SolveArgs& a, cudaStream_t s);
 cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void* fixed_unused,
                                    const int32_t* user_of_internal, void* u_user, cudaStream_t s);
 int solver_vertex_blocks(int n_points);
+// one pass of an iteration on its own: 0 direction, 1 gradient, 2 vertex
+cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s);
 
 }  // namespace agb
 
@@ -96,6 +99,7 @@ struct agb_solver {
   uint32_t* d_ids = nullptr;
   // vertex state
   void* d_x = nullptr;
+  void* d_xlo = nullptr;
   void* d_g = nullptr;
   void* d_d = nullptr;
   void* d_po = nullptr;

@@ -75,6 +75,31 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float rcp_rn(float a) { return __frcp_rn(a); }
 __device__ __forceinline__ double rcp_rn(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// Solver positions are kept as an unevaluated sum hi + lo.  With FP32
+// positions alone, rounding x to 2^-24 |x| caps the reachable ||g||/||g_0||
+// near 1e-5 on stiff meshes (the gradient at the best representable point);
+// the pair carries about 48 bits.  x += b with Knuth's two-sum, renormalised.
+template <class R>
+__device__ __forceinline__ void pair_add(R& hi, R& lo, R b) {
+  const R s = add_rn(hi, b);
+  const R bb = sub_rn(s, hi);
+  const R err = add_rn(sub_rn(hi, sub_rn(s, bb)), sub_rn(b, bb));
+  const R l = add_rn(lo, err);
+  const R h2 = add_rn(s, l);
+  lo = sub_rn(l, sub_rn(h2, s));
+  hi = h2;
+}
+
+// (hi_a + lo_a) - (hi_b + lo_b) rounded once to R
+template <class R>
+__device__ __forceinline__ R pair_diff(R ha, R la, R hb, R lb) {
+  return add_rn(sub_rn(ha, hb), sub_rn(la, lb));
+}
 
 // Jacobi preconditioner entry: 1/|d|, or 1/mean(|d| > 0) where d == 0
 // (benches/bench_pncg_branching_backends.py:407-410)

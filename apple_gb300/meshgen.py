@@ -94,10 +94,12 @@ def grid(nx: int, ny: int, nz: int, h: float = None, lengths=None) -> TetMesh:
     return TetMesh(points=points, cells=cells.astype(np.int32))
 
 
-def ball(n_interior: int, n_shell: int, seed: int = 0, sliver_rel: float = 1e-6) -> TetMesh:
+def ball(n_interior: int, n_shell: int, seed: int = 0, min_quality: float = 0.05) -> TetMesh:
     """Delaunay tetrahedralisation of points uniform in the unit ball plus a
     shell on the unit sphere; vertex order is a seeded random permutation;
-    inverted tets are re-oriented and near-zero-volume slivers dropped."""
+    inverted tets are re-oriented and slivers dropped: quality
+    q = 12 (3V)^(2/3) / sum of squared edge lengths (1 for a regular tet)
+    below ``min_quality`` (about 0.2% of the tets at 0.05)."""
     from scipy.spatial import Delaunay
 
     rng = np.random.default_rng(seed)
@@ -116,7 +118,10 @@ def ball(n_interior: int, n_shell: int, seed: int = 0, sliver_rel: float = 1e-6)
     p = pts[cells]
     D = np.stack([p[:, 1] - p[:, 0], p[:, 2] - p[:, 0], p[:, 3] - p[:, 0]], axis=-1)
     vol = np.linalg.det(D) / 6.0
-    keep = vol > sliver_rel * np.median(vol)
+    edges = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))
+    l2 = sum(((p[:, a] - p[:, b]) ** 2).sum(-1) for a, b in edges)
+    q = 12.0 * np.cbrt(3.0 * np.abs(vol)) ** 2 / l2
+    keep = (vol > 0) & (q >= min_quality)
     cells = cells[keep]
     used = np.zeros(pts.shape[0], bool)
     used[cells.ravel()] = True

@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""PNCG iterations/s on the 1.5M-tet stable Neo-Hookean grid (GB300).
+
+Workload: 50 x 50 x 120 cubes of side 1/50 split 5 tets per cube
+(1,500,000 tets, 314,721 vertices), E = 1e5, nu = 0.49, z = 0 face fixed,
+z = max face displaced +30% of the length along z, FP32 element arithmetic
+with float-float/FP64 reductions.  A step is one PNCG iteration (direction
+pass, gradient pass, vertex pass: one CUDA graph launch); the PNCG state
+carries across steps.  L2 is flushed (256 MiB device write) before every
+timed step; each step is timed with CUDA events on the launching stream.
+
+Also reported: the dominant pass timed alone against the measured HBM peak
+(roofline), the end-to-end rate through the public host-buffer API
+(``minimize_host``: copy u in, solve a fixed number of iterations, copy u
+out), and the CPU baseline (the C/OpenMP FP64 restatement of the reference
+path on this host's cores).
+
+``--impl reference`` times that CPU restatement on the same workload.
+Multi-GPU (torchrun): independent replicas, one per rank (weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NX, NY, NZ = 50, 50, 120
+E_MOD, NU = 1e5, 0.49
+STRETCH = 0.3
+WORKLOAD = "snh_grid_50x50x120_1.5M_tets_stretch30"
+METRIC = "PNCG iters/s at 1.5M tets (stable Neo-Hookean)"
+# algorithmic bytes (per tet: 4 int32 ids + 9 fp32 Dm^-1 + dV + mu + lambda;
+# per vertex per iteration: x, p_prev, g_prev read + x, p, g, diag written)
+B_TET, B_VERT = 64, 84
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-iters", type=int, default=100)
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
+    return ap.parse_args()
+
+
+def _mesh(small=False):
+    from apple_gb300 import meshgen
+
+    nx, ny, nz = (16, 16, 40) if small else (NX, NY, NZ)
+    m = meshgen.grid(nx, ny, nz, h=1.0 / nx)
+    lam, mu = meshgen.lame_converter(E_MOD, NU)
+    import numpy as np
+
+    mask = np.zeros((m.n_points, 3), bool)
+    fv = np.zeros((m.n_points, 3))
+    mask[meshgen.face_mask(m, 2, "min")] = True
+    top = meshgen.face_mask(m, 2, "max")
+    mask[top] = True
+    fv[top, 2] = STRETCH * m.points[:, 2].max()
+    return m, float(mu), float(lam), mask, fv
+
+
+def _measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(gpu_index)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        reasons = sorted({n for r in rows for n, v in zip(self.NAMES, r[5:9]) if v.strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _dist():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def _max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference(steps_req: int, budget: float, small: bool = False) -> dict:
+    """The C/OpenMP FP64 restatement of the reference path on this host."""
+    import numpy as np
+
+    from oracle import build_c
+    from oracle import fem_oracle as O
+
+    m, mu, lam, mask, fv = _mesh(small)
+    dhdX, dV = O.region_compute_grad(m.points, m.cells)
+    cm = build_c.CModel(1, m.cells, dhdX, dV, mu, lam, m.n_points, mask=mask.astype(np.uint8))
+    u0 = np.where(mask, fv, 0.0)
+    t0 = time.perf_counter()
+    cm.pncg(u0, max_steps=1, rtol=0.0)
+    t1 = time.perf_counter() - t0
+    n = int(max(2, min(steps_req, budget / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    _, st = cm.pncg(u0, max_steps=n, rtol=0.0)
+    dt = time.perf_counter() - t0
+    return {"value": st.n_steps / dt, "unit": "iter/s", "cores": build_c.threads(), "kind": "port",
+            "iters": int(st.n_steps), "seconds": dt,
+            "sample": f"{st.n_steps} PNCG iterations of the full {m.n_cells}-tet workload from its initial "
+                      f"state (C/OpenMP FP64 restatement of the reference kernels; one pass per method, "
+                      f"atomic scatter; plus one trailing evaluation)"}
+
+
+def run_reference(a) -> None:
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and rank != 0:
+        return
+    r = cpu_reference(a.steps, max(a.cpu_budget * 3, 30.0), a.small)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": "iter/s", "n_gpus": a.gpus,
+        "steps": r["iters"], "warmup": 1, "ms_per_step": 1e3 / r["value"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "requested_steps": a.steps},
+        "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": r["value"], "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a) -> None:
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import _lib, meshgen
+
+    world, rank, local = _dist()
+    dev = torch.device("cuda", local)
+    m, mu, lam, mask, fv = _mesh(a.small)
+    mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells), mu, lam)
+    b = ag.ModelBuilder(dtype=torch.float32)
+    b.add_vertices(mesh)
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = fv
+    b.add_fixed(mesh)
+    b.add_potential(ag.StableNeoHookean.from_pyvista(mesh))
+    model = b.finalize()
+    nt, nv = m.n_cells, m.n_points
+    u0 = torch.tensor(np.where(mask, fv, 0.0), dtype=torch.float32, device=dev)
+
+    opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=2**30, rtol=0.0))
+    fwd = ag.Forward(model, opt)
+    solver = opt.solver(fwd.problem)
+    solver.reset(u0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    for i in range(a.warmup):
+        flush.fill_(i & 0xFF)
+        solver.step()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    _barrier(world)
+    torch.cuda.synchronize(dev)
+    for i in range(a.steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        solver.step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    _barrier(world)
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in ev]
+    total_s = _max_over_ranks(world, sum(step_ms) / 1e3)
+    state = solver.read()
+    if state.result != ag.Result.UNKNOWN_ERROR:
+        raise RuntimeError(f"solver stopped inside the timed region: {state}")
+    value = world * a.steps / total_s
+    b_iter = nt * B_TET + nv * B_VERT
+
+    # each pass alone, L2 flushed before each launch
+    ms = (ctypes.c_float * 3)()
+    _lib.call("agb_solver_time_passes", solver.handle, 20, ctypes.c_void_p(flush.data_ptr()), flush.numel(),
+              ms, stream.cuda_stream)
+    names = ("direction", "gradient", "vertex")
+    per_launch = {  # algorithmic bytes of one launch of each pass
+        "direction": nt * B_TET + nv * 4 * 12,
+        "gradient": nt * B_TET + nv * 6 * 12,
+        "vertex": nv * 12 * 11,
+    }
+    k = max(range(3), key=lambda i: ms[i])
+    peak, peak_kind = _measured_peak()
+    achieved = per_launch[names[k]] / (ms[k] * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "traffic_per_launch.json"
+    if tp.exists():
+        traffic = json.loads(tp.read_text()).get(names[k])
+
+    # end to end through the public host-buffer API
+    e2e_opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=a.e2e_iters, rtol=0.0))
+    e2e_solver = e2e_opt.solver(ag.ForwardProblem(model))
+    u_host = torch.empty((nv, 3), dtype=torch.float32).pin_memory()
+    base = u0.cpu()
+    times = []
+    for i in range(a.e2e_steps + 1):
+        u_host.copy_(base)
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        sol = e2e_solver.minimize_host(u_host)
+        t1 = time.perf_counter()
+        if i > 0:
+            times.append(t1 - t0)
+        if sol.n_steps != a.e2e_iters:
+            raise RuntimeError(f"e2e solve ran {sol.n_steps} iterations")
+    e2e_s = _max_over_ranks(world, statistics.mean(times))
+    e2e = {"value": world * a.e2e_iters / e2e_s, "unit": "iter/s",
+           "h2d_bytes_per_step": nv * 3 * 4, "d2h_bytes_per_step": nv * 3 * 4 + 160,
+           "iters_per_step": a.e2e_iters, "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        try:
+            r = cpu_reference(10**6, a.cpu_budget, a.small)
+            cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "unit": "iter/s", "cores": None, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * total_s / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD if not a.small else "snh_grid_16x16x40", "n_tets": nt,
+                       "n_vertices": nv, "E": E_MOD, "nu": NU, "step": "one PNCG iteration (one CUDA graph)",
+                       "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}"},
+            "hbm_gbs_algorithmic": b_iter * value / world / 1e9,
+            "roofline": {"bound": "hbm", "kernel": names[k], "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "bytes_per_launch": per_launch[names[k]], "ms_per_launch": ms[k]},
+            "passes_ms": {n: ms[i] for i, n in enumerate(names)},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": 3 * a.steps,
+            "clocks": clk,
+            "step_ms_median": statistics.median(step_ms),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

