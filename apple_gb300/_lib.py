@@ -69,6 +69,7 @@ _SIGNATURES = {
     "agb_fem_hess_diag": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_hess_prod": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_hess_quad": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "agb_fem_fun_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_eval": (
         c_int,
         [c_void_p, c_uint, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],

@@ -115,6 +115,18 @@ int agb_fem_grad(agb_fem* fem, const void* u, void* output, void* stream);
 int agb_fem_hess_diag(agb_fem* fem, const void* u, void* output, void* stream);
 int agb_fem_hess_prod(agb_fem* fem, const void* u, const void* p, void* output, void* stream);
 int agb_fem_hess_quad(agb_fem* fem, const void* u, const void* p, double* output, void* stream);
+/* Allocation-free variant of agb_fem_fun (no counterpart in the reference).
+ * For callers that must not allocate device memory themselves, such as an
+ * XLA/JAX FFI handler running under XLA's allocator (which reserves most of
+ * the device up front) or a loop with a fixed memory budget: u is read in
+ * the caller's order and the per-block partial sums and completion counter
+ * live in one file-scope device array of 512 KiB + 256 B, which holds meshes
+ * of at most 65,536 tiles (larger meshes: AGB_E_INVALID).  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls on a device
+ * share the array; calls that overlap on the GPU race on it.  Accumulates
+ * into output[0] like agb_fem_fun. */
+int agb_fem_fun_noalloc(agb_fem* fem, const void* u, double* output, void* stream);
 /* fused: any subset of AGB_* flags in one pass over the mesh; NULL outputs
  * for unset flags.  p is needed for HESS_PROD and HESS_QUAD. */
 int agb_fem_eval(agb_fem* fem, unsigned flags, const void* u, const void* p, double* energy,
