@@ -46,6 +46,8 @@ struct TilePlan {
   int n_tv = 0;                      // tile-vertex entries (sum over tiles)
   std::vector<int32_t> tile_estart;  // n_tiles + 1, element ranges
   std::vector<int32_t> tile_vstart;  // n_tiles + 1, tile-vertex ranges
+  std::vector<int32_t> tile_gstart;  // n_tiles + 1, warp-group ranges
+  std::vector<int32_t> group_estart; // n_groups + 1, element ranges of conflict-free warp groups
   std::vector<int32_t> tv_vid;       // n_tv, internal vertex id
   std::vector<int32_t> elem_user;    // internal element -> caller's cell index
   std::vector<uint32_t> ids;         // packed 4 x 8-bit local corner ids
@@ -101,6 +103,8 @@ struct FemView {
   int n_cells;
   const int32_t* tile_estart;
   const int32_t* tile_vstart;
+  const int32_t* tile_gstart;
+  const int32_t* group_estart;
   const int32_t* tv_vid;
   // FP32: rec = float4[3][n_cells]; FP64: rec = double[11][n_cells] + ids
   const void* rec;
@@ -118,6 +122,8 @@ struct agb_fem {
   // device
   int32_t* d_tile_estart = nullptr;
   int32_t* d_tile_vstart = nullptr;
+  int32_t* d_tile_gstart = nullptr;
+  int32_t* d_group_estart = nullptr;
   int32_t* d_tv_vid = nullptr;
   int32_t* d_own_slot = nullptr;  // tile-vertex -> slot (standalone)
   int32_t* d_own_off = nullptr;   // n_points + 1

@@ -114,6 +114,8 @@ FemView agb_fem::view() const {
   v.n_cells = plan.n_cells;
   v.tile_estart = d_tile_estart;
   v.tile_vstart = d_tile_vstart;
+  v.tile_gstart = d_tile_gstart;
+  v.group_estart = d_group_estart;
   v.tv_vid = d_tv_vid;
   v.rec = d_rec;
   v.ids = d_ids;
@@ -195,7 +197,8 @@ int agb_region_compute(int32_t n_cells, const int32_t* cells, int32_t n_points,
 // ---------------------------------------------------------------------------
 int agb_fem_destroy(agb_fem* f) {
   if (!f) return AGB_OK;
-  for (void* p : {(void*)f->d_tile_estart, (void*)f->d_tile_vstart, (void*)f->d_tv_vid,
+  for (void* p : {(void*)f->d_tile_estart, (void*)f->d_tile_vstart, (void*)f->d_tile_gstart,
+                  (void*)f->d_group_estart, (void*)f->d_tv_vid,
                   (void*)f->d_own_slot, (void*)f->d_own_off, f->d_rec, (void*)f->d_ids, f->d_u,
                   f->d_p, f->d_slots, (void*)f->d_partials, (void*)f->d_counter})
     dfree(p);
@@ -283,6 +286,8 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
   const size_t n_part = (size_t)std::max(P.n_tiles, unpack_blocks(np)) * 2;
   if (!rc) rc = dupload(&f->d_tile_estart, P.tile_estart);
   if (!rc) rc = dupload(&f->d_tile_vstart, P.tile_vstart);
+  if (!rc) rc = dupload(&f->d_tile_gstart, P.tile_gstart);
+  if (!rc) rc = dupload(&f->d_group_estart, P.group_estart);
   if (!rc) rc = dupload(&f->d_tv_vid, P.tv_vid);
   if (!rc) rc = dupload(&f->d_own_slot, f->own_slots.slot_of_tv);
   if (!rc) rc = dupload(&f->d_own_off, f->own_off);
@@ -518,7 +523,8 @@ int agb_solver_destroy(agb_solver* sv) {
   if (sv->loop_exec) cudaGraphExecDestroy(sv->loop_exec);
   if (sv->step_exec) cudaGraphExecDestroy(sv->step_exec);
   if (sv->capture_stream) cudaStreamDestroy(sv->capture_stream);
-  for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tv_vid,
+  for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tile_gstart,
+                  (void*)sv->d_group_estart, (void*)sv->d_tv_vid,
                   (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_x, sv->d_xlo, sv->d_g, sv->d_d,
                   sv->d_po, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
                   sv->d_u_tmp})
@@ -557,13 +563,17 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
     TilePlan& P = sv->plan;
     P.tile_estart.assign(1, 0);
     P.tile_vstart.assign(1, 0);
+    P.tile_gstart.assign(1, 0);
+    P.group_estart.clear();
     for (size_t k = 0; k < m->fems.size(); ++k) {
       const TilePlan& Q = m->fems[k]->plan;
-      const int eoff = P.n_cells, voff = P.n_tv;
+      const int eoff = P.n_cells, voff = P.n_tv, goff = (int)P.group_estart.size();
       for (int t = 0; t < Q.n_tiles; ++t) {
         P.tile_estart.push_back(eoff + Q.tile_estart[t + 1]);
         P.tile_vstart.push_back(voff + Q.tile_vstart[t + 1]);
+        P.tile_gstart.push_back(goff + Q.tile_gstart[t + 1]);
       }
+      for (size_t g = 0; g + 1 < Q.group_estart.size(); ++g) P.group_estart.push_back(eoff + Q.group_estart[g]);
       P.tv_vid.insert(P.tv_vid.end(), Q.tv_vid.begin(), Q.tv_vid.end());
       P.ids.insert(P.ids.end(), Q.ids.begin(), Q.ids.end());
       P.mudv.insert(P.mudv.end(), Q.mudv.begin(), Q.mudv.end());
@@ -573,6 +583,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
       P.n_tv += Q.n_tv;
       P.n_tiles += Q.n_tiles;
     }
+    P.group_estart.push_back(P.n_cells);
     P.D.assign(9 * (size_t)P.n_cells, 0.0);
     int eoff = 0;
     for (agb_fem* f : m->fems) {
@@ -584,6 +595,8 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
     }
     if (!rc) rc = dupload(&sv->d_tile_estart, P.tile_estart);
     if (!rc) rc = dupload(&sv->d_tile_vstart, P.tile_vstart);
+    if (!rc) rc = dupload(&sv->d_tile_gstart, P.tile_gstart);
+    if (!rc) rc = dupload(&sv->d_group_estart, P.group_estart);
     if (!rc) rc = dupload(&sv->d_tv_vid, P.tv_vid);
     if (!rc) rc = upload_records(P, sv->precision, &sv->d_rec, &sv->d_ids);
     sv->fv.material = mat;
@@ -591,6 +604,8 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
     sv->fv.n_cells = P.n_cells;
     sv->fv.tile_estart = sv->d_tile_estart;
     sv->fv.tile_vstart = sv->d_tile_vstart;
+    sv->fv.tile_gstart = sv->d_tile_gstart;
+    sv->fv.group_estart = sv->d_group_estart;
     sv->fv.tv_vid = sv->d_tv_vid;
     sv->fv.rec = sv->d_rec;
     sv->fv.ids = sv->d_ids;
@@ -599,7 +614,11 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   const size_t v4 = v4_bytes(sv->precision);
   const int vblocks = solver_vertex_blocks(np);
   const size_t nt = (size_t)sv->fv.n_tiles;
-  const size_t n_part = nt * 6 + nt * 1 + (size_t)vblocks * 12 + nt * 3;
+  const size_t gt = (nt + 31) / 32, gv = ((size_t)vblocks + 31) / 32;
+  // partials: direction (nt x 6 + gt x 6), gradient (nt), vertex (vb x 12 + gv x 12), trial (nt x 3 + gt x 3)
+  const size_t off_ga = nt * 6, off_b = off_ga + gt * 6, off_v = off_b + nt, off_gv = off_v + (size_t)vblocks * 12,
+               off_t = off_gv + gv * 12, off_gt = off_t + nt * 3, n_part = off_gt + gt * 3;
+  const size_t n_cnt = (gt + 1) + (gv + 1) + (gt + 1);
   if (!rc) rc = dalloc_bytes(&sv->d_x, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_xlo, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_g, v4 * np);
@@ -607,8 +626,9 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   if (!rc) rc = dalloc_bytes(&sv->d_po, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_slots, v4 * 2 * (size_t)m->n_slots);
   if (!rc) rc = dalloc_bytes(&sv->d_part, 8 * n_part);
-  if (!rc) rc = dalloc(&sv->d_cnt, 4);
-  if (!rc && cudaMemset(sv->d_cnt, 0, 4 * sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
+  if (!rc) rc = dalloc(&sv->d_cnt, n_cnt);
+  if (!rc && cudaMemset(sv->d_cnt, 0, n_cnt * sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
+  if (!rc && solver_prepare_kernels(sv->precision) != cudaSuccess) rc = AGB_E_CUDA;
   if (!rc) rc = dalloc(&sv->d_state, 1);
   if (!rc) rc = dalloc_bytes(&sv->d_u_tmp, 3 * real_bytes(sv->precision) * np);
   if (!rc && cudaMallocHost((void**)&sv->h_state, sizeof(SolverState)) != cudaSuccess) rc = AGB_E_CUDA;
@@ -650,12 +670,15 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.st = sv->d_state;
   char* part = (char*)sv->d_part;
   a.part_a = part;
-  a.part_b = part + 8 * nt * 6;
-  a.part_v = part + 8 * (nt * 7);
-  a.part_t = part + 8 * (nt * 7 + (size_t)vblocks * 12);
+  a.gpart_a = part + 8 * off_ga;
+  a.part_b = part + 8 * off_b;
+  a.part_v = part + 8 * off_v;
+  a.gpart_v = part + 8 * off_gv;
+  a.part_t = part + 8 * off_t;
+  a.gpart_t = part + 8 * off_gt;
   a.cnt_a = sv->d_cnt;
-  a.cnt_v = sv->d_cnt + 1;
-  a.cnt_t = sv->d_cnt + 2;
+  a.cnt_v = sv->d_cnt + (gt + 1);
+  a.cnt_t = sv->d_cnt + (gt + 1) + (gv + 1);
   a.vblocks = vblocks;
   a.max_bt = prm.max_backtracking;
   a.cond = 0;
@@ -744,6 +767,7 @@ int agb_solver_read(agb_solver* sv, void* u_out, agb_pncg_stats* stats, void* st
     RC(check_launch(launch_solver_unpack_x(sv->args, nullptr, sv->model->space->d_user_of_internal,
                                            u_out, s),
                     "unpack_x"));
+  RC(check_launch(launch_solver_energy(sv->args, s), "solver_energy"));
   AGB_CHECK_CUDA(cudaMemcpyAsync(sv->h_state, sv->d_state, sizeof(SolverState),
                                  cudaMemcpyDeviceToHost, s));
   AGB_CHECK_CUDA(cudaStreamSynchronize(s));

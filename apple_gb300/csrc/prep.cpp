@@ -8,6 +8,7 @@
 // each (tile, vertex) pair then owns one slot in a vertex-major CSR that
 // the vertex pass sums in a fixed order.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -123,6 +124,8 @@ int build_tiles(int n_cells, const int32_t* cells, const double* centroid, const
   plan->n_cells = n_cells;
   plan->tile_estart.assign(1, 0);
   plan->tile_vstart.assign(1, 0);
+  plan->tile_gstart.assign(1, 0);
+  plan->group_estart.clear();
   plan->tv_vid.clear();
   plan->elem_user.clear();
   plan->elem_user.reserve(n_cells);
@@ -139,29 +142,124 @@ int build_tiles(int n_cells, const int32_t* cells, const double* centroid, const
     if (tile_elems_list.empty()) return;
     std::sort(tile_verts.begin(), tile_verts.end());
     const int nv = (int)tile_verts.size();
-    std::vector<int32_t> local_of(0);
     // local ids by sorted vertex order
     auto local = [&](int32_t v) {
       return (int)(std::lower_bound(tile_verts.begin(), tile_verts.end(), v) - tile_verts.begin());
     };
-    // element order inside the tile: the 32 elements of a warp-wide step are
-    // spread m apart along the Morton order so that they rarely share a vertex
+    // element order inside the tile: warp groups of <= 32 elements in which
+    // no vertex occurs more than 4 times (first fit along a strided walk of
+    // the Morton order), then, per group, a corner order for every element
+    // such that the elements' corners k = 0..3 are 32 distinct vertices for
+    // each k (a proper 4-edge-colouring of the bipartite element-vertex
+    // incidence graph, which exists since every degree is <= 4).  A warp then
+    // adds the corner-k contributions of its 32 lanes into its own shared
+    // memory copy with plain loads and stores: no atomics, no lost updates.
     const int ne = (int)tile_elems_list.size();
-    const int m = (ne + 31) / 32;
-    for (int c = 0; c < m; ++c)
-      for (int l = 0; l < 32; ++l) {
-        const int idx = l * m + c;
-        if (idx >= ne) continue;
-        const int32_t eu = tile_elems_list[idx];
+    const int stride = (ne + 31) / 32;
+    std::vector<int32_t> walk;
+    walk.reserve(ne);
+    for (int c = 0; c < stride; ++c)
+      for (int l = 0; l < 32; ++l)
+        if (l * stride + c < ne) walk.push_back(tile_elems_list[l * stride + c]);
+    std::vector<std::vector<int32_t>> groups;
+    std::vector<std::array<uint8_t, kTileVerts>> mult;
+    for (const int32_t eu : walk) {
+      int lc[4];
+      for (int a = 0; a < 4; ++a) lc[a] = local(cells[4 * eu + a]);
+      size_t g = 0;
+      for (; g < groups.size(); ++g) {
+        if (groups[g].size() >= 32) continue;
+        bool ok = true;
+        for (int a = 0; a < 4 && ok; ++a) ok = mult[g][lc[a]] < 4;
+        if (ok) break;
+      }
+      if (g == groups.size()) {
+        groups.emplace_back();
+        mult.emplace_back();
+        mult.back().fill(0);
+      }
+      groups[g].push_back(eu);
+      for (int a = 0; a < 4; ++a) ++mult[g][lc[a]];
+    }
+    for (const auto& grp : groups) {
+      const int n = (int)grp.size();
+      // colour[k][a] = position of element k's original corner a
+      std::vector<std::array<int8_t, 4>> pos(n);
+      std::vector<std::array<int, 4>> at_e(n);            // element k, colour c -> vertex or -1
+      std::array<std::array<int, 4>, kTileVerts> at_v;     // vertex, colour -> element or -1
+      for (auto& r : at_e) r.fill(-1);
+      for (auto& r : at_v) r.fill(-1);
+      std::vector<std::array<int, 4>> lc(n);
+      for (int k = 0; k < n; ++k)
+        for (int a = 0; a < 4; ++a) lc[k][a] = local(cells[4 * grp[k] + a]);
+      for (int k = 0; k < n; ++k) {
+        for (int a = 0; a < 4; ++a) {
+          const int v = lc[k][a];
+          int al = 0, be = 0;
+          while (at_e[k][al] >= 0) ++al;  // free at the element
+          while (at_v[v][be] >= 0) ++be;  // free at the vertex
+          if (at_v[v][al] >= 0) {
+            // flip the al/be alternating path that starts at v along colour al
+            std::vector<std::pair<int, int>> path;  // (element, vertex) edges on the path
+            int cv = v, c = al, other = be;
+            while (true) {
+              const int ek = at_v[cv][c];
+              if (ek < 0) break;
+              path.push_back({ek, cv});
+              const int nv2 = at_e[ek][other];
+              if (nv2 < 0) break;
+              path.push_back({ek, nv2});
+              cv = nv2;
+            }
+            // recolour: edges alternate al, be along the path
+            for (size_t q = 0; q < path.size(); ++q) {
+              const int ek = path[q].first, vv = path[q].second;
+              const int cold = (q % 2 == 0) ? al : be;
+              at_e[ek][cold] = -1;
+              at_v[vv][cold] = -1;
+            }
+            for (size_t q = 0; q < path.size(); ++q) {
+              const int ek = path[q].first, vv = path[q].second;
+              const int cnew = (q % 2 == 0) ? be : al;
+              at_e[ek][cnew] = vv;
+              at_v[vv][cnew] = ek;
+            }
+          }
+          at_e[k][al] = v;
+          at_v[v][al] = k;
+        }
+      }
+      plan->group_estart.push_back((int32_t)plan->elem_user.size());
+      for (int k = 0; k < n; ++k) {
+        const int32_t eu = grp[k];
+        // original dhdX rows: row 0 = -(rows 1..3)
+        double R[4][3];
+        for (int j = 0; j < 3; ++j) {
+          R[1][j] = D9[9 * (size_t)eu + j];
+          R[2][j] = D9[9 * (size_t)eu + 3 + j];
+          R[3][j] = D9[9 * (size_t)eu + 6 + j];
+          R[0][j] = -(R[1][j] + R[2][j] + R[3][j]);
+        }
+        int orig_of_pos[4];
+        for (int c = 0; c < 4; ++c) {
+          const int v = at_e[k][c];
+          int a = 0;
+          while (lc[k][a] != v) ++a;
+          orig_of_pos[c] = a;
+        }
         const int ei = (int)plan->elem_user.size();
         plan->elem_user.push_back(eu);
         uint32_t packed = 0;
-        for (int a = 0; a < 4; ++a) packed |= (uint32_t)local(cells[4 * eu + a]) << (8 * a);
+        for (int c = 0; c < 4; ++c) packed |= (uint32_t)lc[k][orig_of_pos[c]] << (8 * c);
         plan->ids[ei] = packed;
-        for (int k = 0; k < 9; ++k) plan->D[(size_t)k * n_cells + ei] = D9[9 * (size_t)eu + k];
+        for (int r = 0; r < 3; ++r)
+          for (int j = 0; j < 3; ++j)
+            plan->D[(size_t)(3 * r + j) * n_cells + ei] = R[orig_of_pos[r + 1]][j];
         plan->mudv[ei] = mudv[eu];
         plan->lamdv[ei] = lamdv ? lamdv[eu] : 0.0;
       }
+    }
+    plan->tile_gstart.push_back((int32_t)plan->group_estart.size());
     for (int i = 0; i < nv; ++i) plan->tv_vid.push_back(tile_verts[i]);
     plan->tile_estart.push_back((int32_t)plan->elem_user.size());
     plan->tile_vstart.push_back((int32_t)plan->tv_vid.size());
@@ -191,6 +289,7 @@ int build_tiles(int n_cells, const int32_t* cells, const double* centroid, const
     tile_elems_list.push_back(e);
   }
   flush();
+  plan->group_estart.push_back((int32_t)plan->elem_user.size());
   plan->n_tiles = (int)plan->tile_estart.size() - 1;
   plan->n_tv = (int)plan->tv_vid.size();
   return AGB_OK;

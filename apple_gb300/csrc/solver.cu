@@ -15,12 +15,17 @@
 //   [ARAP]          trial passes evaluate the remainder at up to three trial
 //                   steps each (ARAP is not polynomial in t)
 //   gradient pass   at x_{k+1} = x_k + t p_k: energy, gradient, clamped
-//                   Hessian diagonal -> tile slots
+//                   Hessian diagonal -> tile slots, accumulated per warp in
+//                   private shared-memory copies (no atomics, fixed order)
 //   vertex pass     x_{k+1}, g_{k+1}, d_{k+1}, p_k written; dot products of
 //                   the Dai-Kou beta, the descent check and the convergence
 //                   norm reduced; the last block decides beta_{k+1}, the
 //                   preconditioner mean and termination, and sets the CUDA
 //                   graph's while-condition.
+// The gradient and vertex passes are launched as programmatic dependents of
+// the pass before them: they read their constant inputs (element records,
+// slot offsets) before griddepcontrol.wait and everything the previous pass
+// writes after it.
 #include <math.h>
 
 #include "kernels.h"
@@ -30,11 +35,29 @@
 namespace agb {
 
 constexpr int kVThreads = 256;
+constexpr int kWarps = kElemThreads / 32;
+// gradient pass: 4 warps per tile, one private accumulator copy per warp
+constexpr int kGradThreads = 128;
+constexpr int kGradWarps = kGradThreads / 32;
+
+// Persistent grids: the vertex pass and the direction pass launch as many
+// CTAs as are resident at once (152 SMs x CTAs per SM) and stride over
+// vertices / tiles, so each CTA's block reduction covers several vertices
+// or tiles and the completion sums a few hundred partials in one level.
+constexpr int kSMs = 152;
+constexpr int kVertexCtasPerSM = 3;
+constexpr int kDirCtasPerSM = 4;
 
 int solver_vertex_blocks(int n_points) {
   int b = (n_points + kVThreads - 1) / kVThreads;
-  return b < 1 ? 1 : (b > 1216 ? 1216 : b);
+  const int cap = kSMs * kVertexCtasPerSM;
+  return b < 1 ? 1 : (b > cap ? cap : b);
 }
+
+static int dir_blocks(int n_tiles) { return n_tiles < kSMs * kDirCtasPerSM ? n_tiles : kSMs * kDirCtasPerSM; }
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 __device__ __forceinline__ double initial_alpha(double gd, double hq, double overstep) {
   double a = -gd / hq;
@@ -115,55 +138,111 @@ __device__ __forceinline__ void position_gradient(R (*sh)[kTileVerts], R (*sl)[k
 // ---------------------------------------------------------------------------
 // direction pass
 // ---------------------------------------------------------------------------
+// positions for the line-search pass: the hi word only (the polynomial's
+// coefficients need ~1e-3 relative accuracy, not the float-float pair)
+template <class R>
+__device__ __forceinline__ void stage_dir(const SolveArgs& a, int vs, int nv, R beta, R inv_mean,
+                                          R (*sx)[kTileVerts], R (*sp)[kTileVerts]) {
+  const V4<R>* X = (const V4<R>*)a.x;
+  const V4<R>* G = (const V4<R>*)a.g;
+  const V4<R>* D = (const V4<R>*)a.d;
+  const V4<R>* PO = (const V4<R>*)a.po;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const int v = a.fv.tv_vid[vs + i];
+    const V4<R> x = ldg4(X + v), g = ldg4(G + v), d = ldg4(D + v), po = ldg4(PO + v);
+    R p[3];
+    pdir(g, d, po, beta, inv_mean, p);
+    sx[0][i] = x.x;
+    sx[1][i] = x.y;
+    sx[2][i] = x.z;
+    sp[0][i] = p[0];
+    sp[1][i] = p[1];
+    sp[2][i] = p[2];
+  }
+}
+
 template <class R, int MAT>
-__global__ void __launch_bounds__(kElemThreads) solver_dir_kernel(SolveArgs a, int use_cond) {
+__global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel(SolveArgs a, int use_cond) {
   constexpr int N = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 6 : 1;
-  __shared__ R sh[3][kTileVerts];
-  __shared__ R sl[3][kTileVerts];
+  // float-float warp trees only for c2 (terms of both signs); p^T H p is a
+  // sum of clamped non-negative terms, c3..c6 are higher-order corrections
+  constexpr unsigned FF = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 0x2u : 0x0u;
+  __shared__ R sx[3][kTileVerts];
   __shared__ R sp[3][kTileVerts];
-  __shared__ Acc<R> red[(kElemThreads / 32) * N];
+  __shared__ Acc<R> red[kWarps * N];
   SolverState* st = a.st;
+  pdl_trigger();
   if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
+  int tile = blockIdx.x;
+  // constant inputs first: the thread's first element record
+  int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  int e = es + threadIdx.x;
+  ElemGeo<R> geo;
+  uint32_t ids = 0;
+  if (e < ee) load_elem<R>(a.fv, e, geo, ids);
   if (st->done) return;
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
-  const int tile = blockIdx.x;
-  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
-  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
-  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sh, sl, sp);
-  __syncthreads();
 
   Acc<R> sums[N] = {};
-  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
-    ElemGeo<R> geo;
-    uint32_t ids;
-    load_elem<R>(a.fv, e, geo, ids);
-    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
-    R w[4][3], G[3][3], dF[3][3];
-    position_gradient(sh, sl, l, geo.D, G);
-    gather_corners(sp, l, w);
-    corner_gradient(w, geo.D, dF);
-    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
-      SnhPoint<R> s;
-      snh_prepare(G, s);
-      SnhDir<R> d;
-      snh_dir(s, dF, d);
-      sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
-      R c[5];
-      snh_poly(s, d, geo.mu, geo.lam, c);
+  for (; tile < a.fv.n_tiles; tile += gridDim.x) {
+    const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+    stage_dir<R>(a, vs, nv, beta, inv_mean, sx, sp);
+    __syncthreads();
+    // next tile of this CTA, for the record prefetch at the end of this one
+    const int tn = tile + gridDim.x;
+    const int esn = tn < a.fv.n_tiles ? a.fv.tile_estart[tn] : 0;
+    const int een = tn < a.fv.n_tiles ? a.fv.tile_estart[tn + 1] : 0;
+    // e walks the thread's elements of this tile (stride blockDim.x); the
+    // record of the following element -- in this tile or the CTA's next
+    // tile -- is loaded while the current one computes
+    const bool had = e < ee;
+    while (e < ee) {
+      int en = e + blockDim.x;
+      const bool last = en >= ee;
+      if (last) en = esn + threadIdx.x;
+      ElemGeo<R> geon;
+      uint32_t idsn = 0;
+      if (last ? en < een : true) load_elem<R>(a.fv, en, geon, idsn);
+      const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+      R w[4][3], G[3][3], dF[3][3];
+      gather_corners(sx, l, w);
+      corner_gradient(w, geo.D, G);
+      gather_corners(sp, l, w);
+      corner_gradient(w, geo.D, dF);
+      if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+        SnhPoint<R> s;
+        snh_prepare(G, s);
+        SnhDir<R> d;
+        snh_dir(s, dF, d);
+        sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
+        R c[5];
+        snh_poly(s, d, geo.mu, geo.lam, c);
 #pragma unroll
-      for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
-    } else {
-      const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
-      Svd<R> sv;
-      svd_rv(G, jm1, sv);
-      R lk[3];
-      arap_lambdas(sv, lk);
-      sums[0].add(fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0)));
+        for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
+      } else {
+        const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
+        Svd<R> sv;
+        svd_rv(G, jm1, sv);
+        R lk[3];
+        arap_lambdas(sv, lk);
+        sums[0].add(fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0)));
+      }
+      geo = geon;
+      ids = idsn;
+      e = en;
+      if (last) break;
     }
+    if (!had) {  // no element of this tile for this thread: start on the next tile
+      e = esn + threadIdx.x;
+      if (e < een) load_elem<R>(a.fv, e, geo, ids);
+    }
+    es = esn;
+    ee = een;
+    __syncthreads();
   }
   double tot[N];
-  if (!grid_reduce<N, R>(sums, (AccStore<R>*)a.part_a, a.cnt_a, gridDim.x, red, tot)) return;
+  if (!grid_reduce_masked<N, FF, R>(sums, (AccStore<R>*)a.part_a, a.cnt_a, gridDim.x, red, tot)) return;
   if (threadIdx.x != 0) return;
   const double hq = tot[0];
   st->hq = hq;
@@ -204,7 +283,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
   __shared__ R sh[3][kTileVerts];
   __shared__ R sl[3][kTileVerts];
   __shared__ R sp[3][kTileVerts];
-  __shared__ Acc<R> red[(kElemThreads / 32) * 3];
+  __shared__ Acc<R> red[kWarps * 3];
   SolverState* st = a.st;
   if (st->done || st->decided) return;
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
@@ -242,7 +321,9 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
     }
   }
   double tot[3];
-  if (!grid_reduce<3, R>(sums, (AccStore<R>*)a.part_t, a.cnt_t, gridDim.x, red, tot)) return;
+  if (!grid_reduce2<3, 0x7u, R>(sums, (AccStore<R>*)a.part_t, (AccStore<R>*)a.gpart_t, a.cnt_t,
+                                gridDim.x, red, tot))
+    return;
   if (threadIdx.x != 0) return;
   const double gd = st->gd;
   for (int j = 0; j < 3; ++j) {
@@ -267,72 +348,124 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
 
 // ---------------------------------------------------------------------------
 // gradient pass at x + t p
+//
+// Elements of a tile come in warp groups (<= 32) whose corner k is a distinct
+// vertex for every lane (host-side edge colouring), so warp w adds its
+// lanes' corner-k contributions into its private copy acc[w] with plain
+// shared-memory loads and stores.  The copies are summed in warp order.
 // ---------------------------------------------------------------------------
+template <class R>
+__host__ __device__ constexpr size_t grad_smem_bytes() {
+  return sizeof(R) * (size_t)kTileVerts * (6 + (size_t)kGradWarps * 6);
+}
+
+size_t solver_grad_smem(int precision) {
+  return precision == AGB_F64 ? grad_smem_bytes<double>() : grad_smem_bytes<float>();
+}
+
 template <class R, int MAT>
-__global__ void __launch_bounds__(kElemThreads) solver_grad_kernel(SolveArgs a) {
-  __shared__ R sh[3][kTileVerts];
-  __shared__ R sl[3][kTileVerts];
-  __shared__ R acc[6][kTileVerts];
-  __shared__ Acc<R> red[kElemThreads / 32];
+__global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 7 : 5) solver_grad_kernel(SolveArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R (*sh)[kTileVerts] = reinterpret_cast<R (*)[kTileVerts]>(smem_raw);
+  R (*sl)[kTileVerts] = sh + 3;
+  R (*acc)[6][kTileVerts] = reinterpret_cast<R (*)[6][kTileVerts]>(sh + 6);
+  __shared__ Acc<R> red[kGradWarps];
+  const int tile = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gs = a.fv.tile_gstart[tile], ge = a.fv.tile_gstart[tile + 1];
+  // constant inputs: the first group's element record
+  int g = gs + warp;
+  int n = 0;
+  ElemGeo<R> geo;
+  uint32_t ids = 0;
+  if (g < ge) {
+    const int e0 = a.fv.group_estart[g];
+    n = a.fv.group_estart[g + 1] - e0;
+    if (lane < n) load_elem<R>(a.fv, e0 + lane, geo, ids);
+  }
+  pdl_trigger();
+  pdl_wait();
   SolverState* st = a.st;
   if (st->done) return;
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean, t = (R)st->t;
-  const int tile = blockIdx.x;
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
-  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
   stage_direction<R>(a, vs, nv, beta, inv_mean, t, false, sh, sl, nullptr);
-  for (int i = threadIdx.x; i < nv; i += blockDim.x)
-#pragma unroll
-    for (int q = 0; q < 6; ++q) acc[q][i] = R(0);
+  {
+    R* accf = &acc[0][0][0];
+    for (int i = threadIdx.x; i < kGradWarps * 6 * kTileVerts; i += blockDim.x) accf[i] = R(0);
+  }
   __syncthreads();
 
   Acc<R> sums[1] = {};
-  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
-    ElemGeo<R> geo;
-    uint32_t ids;
-    load_elem<R>(a.fv, e, geo, ids);
+  while (g < ge) {
+    // prefetch the warp's next group while this one computes
+    const int gn = g + kGradWarps;
+    int nn = 0;
+    ElemGeo<R> geon;
+    uint32_t idsn = 0;
+    if (gn < ge) {
+      const int e0n = a.fv.group_estart[gn];
+      nn = a.fv.group_estart[gn + 1] - e0n;
+      if (lane < nn) load_elem<R>(a.fv, e0n + lane, geon, idsn);
+    }
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
-    R G[3][3], P[3][3], f[4][3];
-    position_gradient(sh, sl, l, geo.D, G);
-    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
-      SnhPoint<R> s;
-      snh_prepare(G, s);
-      sums[0].add(snh_energy(s, geo.mu, geo.lam));
-      snh_pk1(s, geo.mu, geo.lam, P);
-      corner_vjp(P, geo.D, f);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) atomicAdd(&acc[c][l[k]], f[k][c]);
-      snh_hess_diag(s, geo.D, geo.mu, geo.lam, f);
-    } else {
-      const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
-      Svd<R> sv;
-      svd_rv(G, jm1, sv);
-      sums[0].add(arap_energy(sv, geo.mu));
-      arap_pk1(sv, geo.mu, P);
-      corner_vjp(P, geo.D, f);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) atomicAdd(&acc[c][l[k]], f[k][c]);
-      R lk[3];
-      arap_lambdas(sv, lk);
-      arap_hess_diag(sv, lk, geo.D, geo.mu, f);
+    R f[4][3], hd[4][3];
+    if (lane < n) {
+      R G[3][3], P[3][3];
+      position_gradient(sh, sl, l, geo.D, G);
+      if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+        SnhPoint<R> s;
+        snh_prepare(G, s);
+        sums[0].add(snh_energy(s, geo.mu, geo.lam));
+        snh_pk1(s, geo.mu, geo.lam, P);
+        corner_vjp(P, geo.D, f);
+        snh_hess_diag(s, geo.D, geo.mu, geo.lam, hd);
+      } else {
+        const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
+        Svd<R> sv;
+        svd_rv(G, jm1, sv);
+        sums[0].add(arap_energy(sv, geo.mu));
+        arap_pk1(sv, geo.mu, P);
+        corner_vjp(P, geo.D, f);
+        R lk[3];
+        arap_lambdas(sv, lk);
+        arap_hess_diag(sv, lk, geo.D, geo.mu, hd);
+      }
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 4; ++k) {
+      __syncwarp();
+      if (lane < n) {
+        const int v = l[k];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) atomicAdd(&acc[3 + c][l[k]], fmax(f[k][c], R(0)));
+        for (int c = 0; c < 3; ++c) {
+          acc[warp][c][v] += f[k][c];
+          acc[warp][3 + c][v] += fmax(hd[k][c], R(0));
+        }
+      }
+    }
+    __syncwarp();
+    g = gn;
+    n = nn;
+    geo = geon;
+    ids = idsn;
   }
   __syncthreads();
   V4<R>* slots = (V4<R>*)a.slots;
   for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-    const int s = a.slot_of_tv[vs + i];
-    slots[s] = V4<R>{acc[0][i], acc[1][i], acc[2][i], R(0)};
-    slots[(size_t)a.n_slots + s] = V4<R>{acc[3][i], acc[4][i], acc[5][i], R(0)};
+    R q[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      R s = acc[0][c][i];
+#pragma unroll
+      for (int w = 1; w < kGradWarps; ++w) s += acc[w][c][i];
+      q[c] = s;
+    }
+    const int sidx = a.slot_of_tv[vs + i];
+    slots[sidx] = V4<R>{q[0], q[1], q[2], R(0)};
+    slots[(size_t)a.n_slots + sidx] = V4<R>{q[3], q[4], q[5], R(0)};
   }
-  block_reduce<1, R>(sums, red);
+  block_reduce<1, 0x0u, R>(sums, red);
   if (threadIdx.x == 0) ((AccStore<R>*)a.part_b)[blockIdx.x] = acc_store(sums[0]);
 }
 
@@ -343,6 +476,14 @@ template <class R>
 __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, int use_cond) {
   constexpr int N = 12;
   __shared__ Acc<R> red[(kVThreads / 32) * N];
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  // constant inputs before the dependency wait
+  int s0 = 0, s1 = 0;
+  if (i0 < a.n_points) {
+    s0 = a.off[i0];
+    s1 = a.off[i0 + 1];
+  }
+  pdl_wait();
   SolverState* st = a.st;
   if (st->done) {
     if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
@@ -359,7 +500,11 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   const V4<R>* slots = (const V4<R>*)a.slots;
   // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
   Acc<R> s[N] = {};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) {
+  for (int i = i0; i < a.n_points; i += gridDim.x * blockDim.x) {
+    if (i != i0) {
+      s0 = a.off[i];
+      s1 = a.off[i + 1];
+    }
     const V4<R> x = X[i], xl = XL[i], g = Gv[i], d = Dv[i], po = PO[i];
     const int mask = (int)x.w;
     R p[3];
@@ -369,7 +514,7 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
     for (int c = 0; c < 3; ++c) pair_add(xh[c], xlo[c], mul_rn(t, p[c]));
     const R xn[3] = {xh[0] + xlo[0], xh[1] + xlo[1], xh[2] + xlo[2]};
     R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
-    for (int k = a.off[i]; k < a.off[i + 1]; ++k) {
+    for (int k = s0; k < s1; ++k) {
       const V4<R> sg = slots[k], sd = slots[(size_t)a.n_slots + k];
       gs[0] += sg.x;
       gs[1] += sg.y;
@@ -418,9 +563,9 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
     PO[i] = V4<R>{p[0], p[1], p[2], R(0)};
   }
   double tot[N];
-  if (!grid_reduce<N, R>(s, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
-  const double elastic =
-      block_sum_partials<R>((const AccStore<R>*)a.part_b, a.fv.n_tiles, 1, red);
+  // float-float warp trees for the sums whose terms change sign
+  constexpr unsigned FF = (1u << 1) | (1u << 6) | (1u << 8) | (1u << 9);
+  if (!grid_reduce_masked<N, FF, R>(s, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
   if (threadIdx.x != 0) return;
   const double cnt = tot[4], sad = tot[3];
   const double inv_m = (cnt > 0.0 && sad > 0.0) ? cnt / sad : 1.0;
@@ -429,7 +574,6 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   const double yPy = tot[2] + inv_m * tot[7];
   const double yp = tot[8], pg = tot[9], gg = tot[10];
   const double gnorm = sqrt(gg);
-  const double energy = elastic + tot[11];
   const bool first = st->init != 0;
   double b = 0.0;
   if (!first) {
@@ -445,7 +589,7 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   st->inv_mean = inv_m;
   st->gd = gd;
   st->gnorm = gnorm;
-  st->energy = energy;
+  st->ext_energy = tot[11];
   st->reset_beta = 0;
   if (first) {
     st->gnorm0 = gnorm;
@@ -454,7 +598,7 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
     st->iter += 1;
   }
   int result = AGB_RUNNING;
-  if (!isfinite(gnorm) || !isfinite(energy))
+  if (!isfinite(gnorm) || !isfinite(gPg) || !isfinite(tot[11]))
     result = AGB_NAN_ENCOUNTERED;
   else if (!first && st->ls_fail)
     result = AGB_LINE_SEARCH_FAILED;
@@ -469,6 +613,14 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   if (use_cond)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
                             (!st->done && st->iter < st->iter_limit) ? 1u : 0u);
+}
+
+// total energy at x: gradient-pass partials + external work (on demand)
+template <class R>
+__global__ void __launch_bounds__(256) solver_energy_kernel(SolveArgs a) {
+  __shared__ Acc<R> red[8];
+  const double e = block_sum_partials<R>((const AccStore<R>*)a.part_b, a.fv.n_tiles, 1, red);
+  if (threadIdx.x == 0) a.st->energy = e + a.st->ext_energy;
 }
 
 // ---------------------------------------------------------------------------
@@ -502,6 +654,7 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     st->gnorm = 0.0;
     st->gnorm0 = 0.0;
     st->energy = 0.0;
+    st->ext_energy = 0.0;
     st->delta_e = 0.0;
     st->iter = 0;
     st->iter_limit = 0;
@@ -531,6 +684,26 @@ __global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ x, const V
   }
 }
 
+cudaError_t solver_prepare_kernels(int precision) {
+  cudaError_t e;
+  if (precision == AGB_F64) {
+    const int bytes = (int)grad_smem_bytes<double>();
+    e = cudaFuncSetAttribute(solver_grad_kernel<double, AGB_ARAP>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(solver_grad_kernel<double, AGB_STABLE_NEO_HOOKEAN>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  } else {
+    const int bytes = (int)grad_smem_bytes<float>();
+    e = cudaFuncSetAttribute(solver_grad_kernel<float, AGB_ARAP>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(solver_grad_kernel<float, AGB_STABLE_NEO_HOOKEAN>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+  return e;
+}
+
 cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,
                                const int32_t* uoi, cudaStream_t s) {
   const int blocks = solver_vertex_blocks(a.n_points);
@@ -548,58 +721,82 @@ cudaError_t launch_solver_set_limit(const SolveArgs& a, int n_steps, cudaStream_
   return cudaGetLastError();
 }
 
+cudaError_t launch_solver_energy(const SolveArgs& a, cudaStream_t s) {
+  if (a.precision == AGB_F64)
+    solver_energy_kernel<double><<<1, 256, 0, s>>>(a);
+  else
+    solver_energy_kernel<float><<<1, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// launch with programmatic stream serialisation: the kernel may start while
+// the previous kernel in the stream finishes and waits in griddepcontrol.wait
+template <class... P, class... A>
+static cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              A... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 template <class R, int MAT>
-static void launch_iteration_t(const SolveArgs& a, bool use_cond, bool first, int max_bt,
-                               cudaStream_t s) {
+static cudaError_t launch_iteration_t(const SolveArgs& a, bool use_cond, bool first, int max_bt,
+                                      cudaStream_t s) {
   const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
   if (!first) {
-    solver_dir_kernel<R, MAT><<<eg, eb, 0, s>>>(a, use_cond ? 1 : 0);
+    solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, use_cond ? 1 : 0);
     if constexpr (MAT == AGB_ARAP) {
       for (int j0 = 0; j0 <= max_bt; j0 += 3) solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0);
     }
   }
-  solver_grad_kernel<R, MAT><<<eg, eb, 0, s>>>(a);
-  solver_vertex_kernel<R><<<a.vblocks, kVThreads, 0, s>>>(a, use_cond ? 1 : 0);
+  cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a);
+  if (e != cudaSuccess) return e;
+  return launch_pdl(solver_vertex_kernel<R>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond ? 1 : 0);
 }
 
 static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool first, cudaStream_t s) {
-  const int max_bt = a.max_bt;
   if (a.fv.n_tiles == 0) return cudaErrorInvalidValue;
+  const int max_bt = a.max_bt;
+  cudaError_t e;
   if (a.precision == AGB_F64) {
     if (a.fv.material == AGB_ARAP)
-      launch_iteration_t<double, AGB_ARAP>(a, use_cond, first, max_bt, s);
+      e = launch_iteration_t<double, AGB_ARAP>(a, use_cond, first, max_bt, s);
     else
-      launch_iteration_t<double, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
+      e = launch_iteration_t<double, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
   } else {
     if (a.fv.material == AGB_ARAP)
-      launch_iteration_t<float, AGB_ARAP>(a, use_cond, first, max_bt, s);
+      e = launch_iteration_t<float, AGB_ARAP>(a, use_cond, first, max_bt, s);
     else
-      launch_iteration_t<float, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
+      e = launch_iteration_t<float, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
   }
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
 template <class R, int MAT>
-static void launch_pass_t(const SolveArgs& a, int which, cudaStream_t s) {
+static cudaError_t launch_pass_t(const SolveArgs& a, int which, cudaStream_t s) {
   const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
-  if (which == 0) solver_dir_kernel<R, MAT><<<eg, eb, 0, s>>>(a, 0);
-  if (which == 1) solver_grad_kernel<R, MAT><<<eg, eb, 0, s>>>(a);
+  if (which == 0) solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, 0);
+  if (which == 1) solver_grad_kernel<R, MAT><<<eg, kGradThreads, grad_smem_bytes<R>(), s>>>(a);
   if (which == 2) solver_vertex_kernel<R><<<a.vblocks, kVThreads, 0, s>>>(a, 0);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s) {
   if (a.precision == AGB_F64) {
-    if (a.fv.material == AGB_ARAP)
-      launch_pass_t<double, AGB_ARAP>(a, which, s);
-    else
-      launch_pass_t<double, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
-  } else {
-    if (a.fv.material == AGB_ARAP)
-      launch_pass_t<float, AGB_ARAP>(a, which, s);
-    else
-      launch_pass_t<float, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
+    if (a.fv.material == AGB_ARAP) return launch_pass_t<double, AGB_ARAP>(a, which, s);
+    return launch_pass_t<double, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
   }
-  return cudaGetLastError();
+  if (a.fv.material == AGB_ARAP) return launch_pass_t<float, AGB_ARAP>(a, which, s);
+  return launch_pass_t<float, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
 }
 
 cudaError_t launch_solver_iteration(const SolveArgs& a, bool use_cond, cudaStream_t s) {

@@ -21,7 +21,8 @@ struct SolverState {
   double hq;        // clamped p^T H p
   double gnorm;     // ||g|| over free DOFs at x
   double gnorm0;
-  double energy;    // total energy at x
+  double energy;    // total energy at x (summed on demand, see solver_energy)
+  double ext_energy;  // external-force work term at x
   double delta_e;   // predicted energy change of the accepted step
   // parameters
   double rtol, atol, armijo_c, overstep, beta_max;
@@ -57,13 +58,16 @@ struct SolveArgs {
   void* slots;         // V4<R> [2][n_slots]
   int32_t n_slots;
   SolverState* st;
-  void* part_a;        // direction-pass partials (n_tiles x 6)
-  void* part_b;        // gradient-pass partials (n_tiles x 1)
-  void* part_v;        // vertex-pass partials (vblocks x 12)
-  void* part_t;        // ARAP trial partials (n_tiles x 3)
-  unsigned* cnt_a;
-  unsigned* cnt_v;
-  unsigned* cnt_t;
+  void* part_a;        // direction-pass partials (n_tiles x 6) and group partials
+  void* gpart_a;
+  void* part_b;        // gradient-pass energy partials (n_tiles x 1)
+  void* part_v;        // vertex-pass partials (vblocks x 12) and group partials
+  void* gpart_v;
+  void* part_t;        // ARAP trial partials (n_tiles x 3) and group partials
+  void* gpart_t;
+  unsigned* cnt_a;     // ceil(n_tiles/32) + 1 completion counters
+  unsigned* cnt_v;     // ceil(vblocks/32) + 1
+  unsigned* cnt_t;     // ceil(n_tiles/32) + 1
   int vblocks;
   int max_bt;               // Armijo halvings (ARAP trial passes launched)
   unsigned long long cond;  // cudaGraphConditionalHandle or 0
@@ -79,6 +83,12 @@ cudaError_t launch_solver_first(const SolveArgs& a, cudaStream_t s);
 cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void* fixed_unused,
                                    const int32_t* user_of_internal, void* u_user, cudaStream_t s);
 int solver_vertex_blocks(int n_points);
+// set kernel attributes (dynamic shared memory of the gradient pass); call
+// once before launching or capturing solver kernels
+cudaError_t solver_prepare_kernels(int precision);
+// sum the gradient pass's energy partials and the external work into st->energy
+cudaError_t launch_solver_energy(const SolveArgs& a, cudaStream_t s);
+size_t solver_grad_smem(int precision);
 // one pass of an iteration on its own: 0 direction, 1 gradient, 2 vertex
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s);
 
@@ -93,6 +103,8 @@ struct agb_solver {
   agb::TilePlan plan;
   int32_t* d_tile_estart = nullptr;
   int32_t* d_tile_vstart = nullptr;
+  int32_t* d_tile_gstart = nullptr;
+  int32_t* d_group_estart = nullptr;
   int32_t* d_tv_vid = nullptr;
   int32_t* d_slot_of_tv = nullptr;
   void* d_rec = nullptr;
