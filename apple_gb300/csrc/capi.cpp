@@ -525,8 +525,8 @@ int agb_solver_destroy(agb_solver* sv) {
   if (sv->capture_stream) cudaStreamDestroy(sv->capture_stream);
   for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tile_gstart,
                   (void*)sv->d_group_estart, (void*)sv->d_tv_vid,
-                  (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_x, sv->d_xlo, sv->d_g, sv->d_d,
-                  sv->d_po, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
+                  (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_xa, sv->d_gd, sv->d_p0,
+                  sv->d_p1, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
                   sv->d_u_tmp})
     dfree(p);
   if (sv->h_state) cudaFreeHost(sv->h_state);
@@ -619,11 +619,10 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   const size_t off_ga = nt * 6, off_b = off_ga + gt * 6, off_v = off_b + nt, off_gv = off_v + (size_t)vblocks * 12,
                off_t = off_gv + gv * 12, off_gt = off_t + nt * 3, n_part = off_gt + gt * 3;
   const size_t n_cnt = (gt + 1) + (gv + 1) + (gt + 1);
-  if (!rc) rc = dalloc_bytes(&sv->d_x, v4 * np);
-  if (!rc) rc = dalloc_bytes(&sv->d_xlo, v4 * np);
-  if (!rc) rc = dalloc_bytes(&sv->d_g, v4 * np);
-  if (!rc) rc = dalloc_bytes(&sv->d_d, v4 * np);
-  if (!rc) rc = dalloc_bytes(&sv->d_po, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_xa, 2 * v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_gd, 2 * v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_p0, v4 * np);
+  if (!rc) rc = dalloc_bytes(&sv->d_p1, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_slots, v4 * 2 * (size_t)m->n_slots);
   if (!rc) rc = dalloc_bytes(&sv->d_part, 8 * n_part);
   if (!rc) rc = dalloc(&sv->d_cnt, n_cnt);
@@ -657,11 +656,10 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.fv = sv->fv;
   a.n_points = np;
   a.precision = sv->precision;
-  a.x = sv->d_x;
-  a.xlo = sv->d_xlo;
-  a.g = sv->d_g;
-  a.d = sv->d_d;
-  a.po = sv->d_po;
+  a.xa = sv->d_xa;
+  a.gd = sv->d_gd;
+  a.p0 = sv->d_p0;
+  a.p1 = sv->d_p1;
   a.force = m->d_force;
   a.slot_of_tv = sv->d_slot_of_tv;
   a.off = m->d_off;

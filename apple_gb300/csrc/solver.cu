@@ -45,8 +45,8 @@ constexpr int kGradWarps = kGradThreads / 32;
 // vertices / tiles, so each CTA's block reduction covers several vertices
 // or tiles and the completion sums a few hundred partials in one level.
 constexpr int kSMs = 152;
-constexpr int kVertexCtasPerSM = 3;
-constexpr int kDirCtasPerSM = 4;
+constexpr int kVertexCtasPerSM = 4;
+constexpr int kDirCtasPerSM = 3;
 
 int solver_vertex_blocks(int n_points) {
   int b = (n_points + kVThreads - 1) / kVThreads;
@@ -78,36 +78,33 @@ __device__ __forceinline__ void reject_step(SolverState* st, int ls) {
   if (st->beta == 0.0) st->ls_fail = 1;
 }
 
+// search directions: p[pbuf] = p_prev, p[pbuf ^ 1] = p of this iteration
 template <class R>
-__device__ __forceinline__ void stage_direction(const SolveArgs& a, int vs, int nv, R beta,
-                                                R inv_mean, R t, bool want_p, R (*sh)[kTileVerts],
-                                                R (*sl)[kTileVerts], R (*sp)[kTileVerts]) {
-  const V4<R>* X = (const V4<R>*)a.x;
-  const V4<R>* XL = (const V4<R>*)a.xlo;
-  const V4<R>* G = (const V4<R>*)a.g;
-  const V4<R>* D = (const V4<R>*)a.d;
-  const V4<R>* PO = (const V4<R>*)a.po;
+__device__ __forceinline__ V4<R>* p_prev(const SolveArgs& a, int pb) {
+  return (V4<R>*)(pb ? a.p1 : a.p0);
+}
+template <class R>
+__device__ __forceinline__ V4<R>* p_cur(const SolveArgs& a, int pb) {
+  return (V4<R>*)(pb ? a.p0 : a.p1);
+}
+
+template <class R>
+__device__ __forceinline__ void stage_direction(const SolveArgs& a, int vs, int nv, const V4<R>* P,
+                                                R (*sh)[kTileVerts], R (*sl)[kTileVerts],
+                                                R (*sp)[kTileVerts]) {
+  const V4<R>* XA = (const V4<R>*)a.xa;
   for (int i = threadIdx.x; i < nv; i += blockDim.x) {
     const int v = a.fv.tv_vid[vs + i];
-    const V4<R> x = ldg4(X + v), xl = ldg4(XL + v), g = ldg4(G + v), d = ldg4(D + v),
-                po = ldg4(PO + v);
-    R p[3];
-    pdir(g, d, po, beta, inv_mean, p);
-    R hx = x.x, lx = xl.x, hy = x.y, ly = xl.y, hz = x.z, lz = xl.z;
-    pair_add(hx, lx, mul_rn(t, p[0]));
-    pair_add(hy, ly, mul_rn(t, p[1]));
-    pair_add(hz, lz, mul_rn(t, p[2]));
-    sh[0][i] = hx;
-    sh[1][i] = hy;
-    sh[2][i] = hz;
-    sl[0][i] = lx;
-    sl[1][i] = ly;
-    sl[2][i] = lz;
-    if (want_p) {
-      sp[0][i] = p[0];
-      sp[1][i] = p[1];
-      sp[2][i] = p[2];
-    }
+    const V4<R> x = ldg4(XA + 2 * v), xl = ldg4(XA + 2 * v + 1), p = ldg4(P + v);
+    sh[0][i] = x.x;
+    sh[1][i] = x.y;
+    sh[2][i] = x.z;
+    sl[0][i] = xl.x;
+    sl[1][i] = xl.y;
+    sl[2][i] = xl.z;
+    sp[0][i] = p.x;
+    sp[1][i] = p.y;
+    sp[2][i] = p.z;
   }
 }
 
@@ -139,26 +136,44 @@ __device__ __forceinline__ void position_gradient(R (*sh)[kTileVerts], R (*sl)[k
 // direction pass
 // ---------------------------------------------------------------------------
 // positions for the line-search pass: the hi word only (the polynomial's
-// coefficients need ~1e-3 relative accuracy, not the float-float pair)
+// coefficients need ~1e-3 relative accuracy, not the float-float pair);
+// one 16-byte vector per vertex so a corner is one shared-memory load
+// p = -P g + beta p_prev for the thread's tile vertex v (kTileVerts ==
+// kElemThreads; v < 0: none): staged with x_hi for the tile's elements and
+// stored as this iteration's direction (tiles sharing v store equal values)
 template <class R>
-__device__ __forceinline__ void stage_dir(const SolveArgs& a, int vs, int nv, R beta, R inv_mean,
-                                          R (*sx)[kTileVerts], R (*sp)[kTileVerts]) {
-  const V4<R>* X = (const V4<R>*)a.x;
-  const V4<R>* G = (const V4<R>*)a.g;
-  const V4<R>* D = (const V4<R>*)a.d;
-  const V4<R>* PO = (const V4<R>*)a.po;
-  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-    const int v = a.fv.tv_vid[vs + i];
-    const V4<R> x = ldg4(X + v), g = ldg4(G + v), d = ldg4(D + v), po = ldg4(PO + v);
-    R p[3];
-    pdir(g, d, po, beta, inv_mean, p);
-    sx[0][i] = x.x;
-    sx[1][i] = x.y;
-    sx[2][i] = x.z;
-    sp[0][i] = p[0];
-    sp[1][i] = p[1];
-    sp[2][i] = p[2];
-  }
+__device__ __forceinline__ void stage_dir(const SolveArgs& a, int v, R beta, R inv_mean,
+                                          const V4<R>* pprev, V4<R>* pcur, V4<R>* sx, V4<R>* sp) {
+  if (v < 0) return;
+  const V4<R> x = ldg4((const V4<R>*)a.xa + 2 * v), g = ldg4((const V4<R>*)a.gd + 2 * v),
+              d = ldg4((const V4<R>*)a.gd + 2 * v + 1), po = ldg4(pprev + v);
+  R p[3];
+  pdir(g, d, po, beta, inv_mean, p);
+  const V4<R> pv{p[0], p[1], p[2], R(0)};
+  pcur[v] = pv;
+  sx[threadIdx.x] = V4<R>{x.x, x.y, x.z, R(0)};
+  sp[threadIdx.x] = pv;
+}
+
+// the thread's vertex of a tile, or -1
+__device__ __forceinline__ int tile_vertex(const FemView& fv, int tile, int i) {
+  if (tile >= fv.n_tiles) return -1;
+  const int vs = fv.tile_vstart[tile];
+  return i < fv.tile_vstart[tile + 1] - vs ? fv.tv_vid[vs + i] : -1;
+}
+
+// W = sum_a (w_a - w_0) D_a^T from 16-byte staged corners
+template <class R>
+__device__ __forceinline__ void vec_gradient(const V4<R>* s, const int (&l)[4], const R (&D)[3][3],
+                                             R (&W)[3][3]) {
+  const V4<R> w0 = s[l[0]], w1 = s[l[1]], w2 = s[l[2]], w3 = s[l[3]];
+  const R e[3][3] = {{w1.x - w0.x, w2.x - w0.x, w3.x - w0.x},
+                     {w1.y - w0.y, w2.y - w0.y, w3.y - w0.y},
+                     {w1.z - w0.z, w2.z - w0.z, w3.z - w0.z}};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) W[i][j] = e[i][0] * D[0][j] + e[i][1] * D[1][j] + e[i][2] * D[2][j];
 }
 
 template <class R, int MAT>
@@ -167,27 +182,33 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   // float-float warp trees only for c2 (terms of both signs); p^T H p is a
   // sum of clamped non-negative terms, c3..c6 are higher-order corrections
   constexpr unsigned FF = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 0x2u : 0x0u;
-  __shared__ R sx[3][kTileVerts];
-  __shared__ R sp[3][kTileVerts];
+  __shared__ V4<R> sx[kTileVerts];
+  __shared__ V4<R> sp[kTileVerts];
   __shared__ Acc<R> red[kWarps * N];
   SolverState* st = a.st;
   pdl_trigger();
   if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
+  static_assert(kTileVerts == kElemThreads, "one staged vertex per thread");
   int tile = blockIdx.x;
-  // constant inputs first: the thread's first element record
+  // constant inputs first: the thread's first element record and vertex id
   int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
   int e = es + threadIdx.x;
   ElemGeo<R> geo;
   uint32_t ids = 0;
   if (e < ee) load_elem<R>(a.fv, e, geo, ids);
+  int vid = tile_vertex(a.fv, tile, threadIdx.x);
   if (st->done) return;
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
+  const int pb = st->pbuf;
+  const V4<R>* pprev = p_prev<R>(a, pb);
+  V4<R>* pcur = p_cur<R>(a, pb);
 
   Acc<R> sums[N] = {};
   for (; tile < a.fv.n_tiles; tile += gridDim.x) {
-    const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
-    stage_dir<R>(a, vs, nv, beta, inv_mean, sx, sp);
+    stage_dir<R>(a, vid, beta, inv_mean, pprev, pcur, sx, sp);
+    // the next tile's vertex id, in flight while this tile computes
+    vid = tile_vertex(a.fv, tile + gridDim.x, threadIdx.x);
     __syncthreads();
     // next tile of this CTA, for the record prefetch at the end of this one
     const int tn = tile + gridDim.x;
@@ -205,11 +226,9 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
       uint32_t idsn = 0;
       if (last ? en < een : true) load_elem<R>(a.fv, en, geon, idsn);
       const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
-      R w[4][3], G[3][3], dF[3][3];
-      gather_corners(sx, l, w);
-      corner_gradient(w, geo.D, G);
-      gather_corners(sp, l, w);
-      corner_gradient(w, geo.D, dF);
+      R G[3][3], dF[3][3];
+      vec_gradient(sx, l, geo.D, G);
+      vec_gradient(sp, l, geo.D, dF);
       if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
         SnhPoint<R> s;
         snh_prepare(G, s);
@@ -286,7 +305,6 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
   __shared__ Acc<R> red[kWarps * 3];
   SolverState* st = a.st;
   if (st->done || st->decided) return;
-  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
   const double a0 = st->alpha0;
   R tj[3];
 #pragma unroll
@@ -294,7 +312,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
   const int tile = blockIdx.x;
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
-  stage_direction<R>(a, vs, nv, beta, inv_mean, R(0), true, sh, sl, sp);
+  stage_direction<R>(a, vs, nv, p_cur<R>(a, st->pbuf), sh, sl, sp);
   __syncthreads();
   Acc<R> sums[3] = {};
   for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
@@ -356,19 +374,63 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
 // ---------------------------------------------------------------------------
 template <class R>
 __host__ __device__ constexpr size_t grad_smem_bytes() {
-  return sizeof(R) * (size_t)kTileVerts * (6 + (size_t)kGradWarps * 6);
+  // staged hi (V4: x y z lo.x) and lo (V2: lo.y lo.z) + per-warp accumulators (V4 + V2)
+  return (size_t)kTileVerts * (size_t)(kGradWarps + 1) * (sizeof(V4<R>) + sizeof(V2<R>));
 }
 
 size_t solver_grad_smem(int precision) {
   return precision == AGB_F64 ? grad_smem_bytes<double>() : grad_smem_bytes<float>();
 }
 
+// x + t p as hi + lo pairs: (hi.x hi.y hi.z lo.x) and (lo.y lo.z) per vertex
+constexpr int kGradVerts = kTileVerts / kGradThreads;  // staged vertices per thread
+
+template <class R>
+__device__ __forceinline__ void stage_point(const SolveArgs& a, const int (&vid)[kGradVerts], const V4<R>* P,
+                                            R t, V4<R>* sh, V2<R>* sl) {
+  const V4<R>* XA = (const V4<R>*)a.xa;
+#pragma unroll
+  for (int j = 0; j < kGradVerts; ++j) {
+    const int v = vid[j], i = threadIdx.x + j * kGradThreads;
+    if (v < 0) continue;
+    const V4<R> x = ldg4(XA + 2 * v), xl = ldg4(XA + 2 * v + 1), p = ldg4(P + v);
+    R hx = x.x, lx = xl.x, hy = x.y, ly = xl.y, hz = x.z, lz = xl.z;
+    pair_add(hx, lx, mul_rn(t, p.x));
+    pair_add(hy, ly, mul_rn(t, p.y));
+    pair_add(hz, lz, mul_rn(t, p.z));
+    sh[i] = V4<R>{hx, hy, hz, lx};
+    sl[i] = V2<R>{ly, lz};
+  }
+}
+
+// G = sum_a (x_a - x_0) D_a^T with the differences taken on hi + lo pairs
+template <class R>
+__device__ __forceinline__ void pair_gradient(const V4<R>* sh, const V2<R>* sl, const int (&l)[4],
+                                              const R (&D)[3][3], R (&G)[3][3]) {
+  const V4<R> h0 = sh[l[0]];
+  const V2<R> q0 = sl[l[0]];
+  R e[3][3];
+#pragma unroll
+  for (int a = 1; a < 4; ++a) {
+    const V4<R> h = sh[l[a]];
+    const V2<R> q = sl[l[a]];
+    e[0][a - 1] = pair_diff(h.x, h.w, h0.x, h0.w);
+    e[1][a - 1] = pair_diff(h.y, q.x, h0.y, q0.x);
+    e[2][a - 1] = pair_diff(h.z, q.y, h0.z, q0.y);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) G[i][j] = e[i][0] * D[0][j] + e[i][1] * D[1][j] + e[i][2] * D[2][j];
+}
+
 template <class R, int MAT>
 __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 7 : 5) solver_grad_kernel(SolveArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R (*sh)[kTileVerts] = reinterpret_cast<R (*)[kTileVerts]>(smem_raw);
-  R (*sl)[kTileVerts] = sh + 3;
-  R (*acc)[6][kTileVerts] = reinterpret_cast<R (*)[6][kTileVerts]>(sh + 6);
+  V4<R>* sh = reinterpret_cast<V4<R>*>(smem_raw);
+  V4<R>* acc4 = sh + kTileVerts;  // [warp][vertex]: gx gy gz dx
+  V2<R>* sl = reinterpret_cast<V2<R>*>(acc4 + kGradWarps * kTileVerts);
+  V2<R>* acc2 = sl + kTileVerts;  // [warp][vertex]: dy dz
   __shared__ Acc<R> red[kGradWarps];
   const int tile = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -383,19 +445,27 @@ __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 
     n = a.fv.group_estart[g + 1] - e0;
     if (lane < n) load_elem<R>(a.fv, e0 + lane, geo, ids);
   }
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  int vid[kGradVerts], sidx[kGradVerts];
+#pragma unroll
+  for (int j = 0; j < kGradVerts; ++j) {
+    const int i = threadIdx.x + j * kGradThreads;
+    vid[j] = i < nv ? a.fv.tv_vid[vs + i] : -1;
+    sidx[j] = i < nv ? a.slot_of_tv[vs + i] : 0;
+  }
   pdl_trigger();
   pdl_wait();
   SolverState* st = a.st;
   if (st->done) return;
-  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean, t = (R)st->t;
-  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
-  stage_direction<R>(a, vs, nv, beta, inv_mean, t, false, sh, sl, nullptr);
-  {
-    R* accf = &acc[0][0][0];
-    for (int i = threadIdx.x; i < kGradWarps * 6 * kTileVerts; i += blockDim.x) accf[i] = R(0);
+  stage_point<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
+  for (int i = threadIdx.x; i < kGradWarps * kTileVerts; i += blockDim.x) {
+    acc4[i] = V4<R>{R(0), R(0), R(0), R(0)};
+    acc2[i] = V2<R>{R(0), R(0)};
   }
   __syncthreads();
 
+  V4<R>* my4 = acc4 + warp * kTileVerts;
+  V2<R>* my2 = acc2 + warp * kTileVerts;
   Acc<R> sums[1] = {};
   while (g < ge) {
     // prefetch the warp's next group while this one computes
@@ -412,7 +482,7 @@ __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 
     R f[4][3], hd[4][3];
     if (lane < n) {
       R G[3][3], P[3][3];
-      position_gradient(sh, sl, l, geo.D, G);
+      pair_gradient(sh, sl, l, geo.D, G);
       if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
         SnhPoint<R> s;
         snh_prepare(G, s);
@@ -437,11 +507,16 @@ __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 
       __syncwarp();
       if (lane < n) {
         const int v = l[k];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          acc[warp][c][v] += f[k][c];
-          acc[warp][3 + c][v] += fmax(hd[k][c], R(0));
-        }
+        V4<R> q4 = my4[v];
+        V2<R> q2 = my2[v];
+        q4.x += f[k][0];
+        q4.y += f[k][1];
+        q4.z += f[k][2];
+        q4.w += fmax(hd[k][0], R(0));
+        q2.x += fmax(hd[k][1], R(0));
+        q2.y += fmax(hd[k][2], R(0));
+        my4[v] = q4;
+        my2[v] = q2;
       }
     }
     __syncwarp();
@@ -452,18 +527,25 @@ __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 
   }
   __syncthreads();
   V4<R>* slots = (V4<R>*)a.slots;
-  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-    R q[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      R s = acc[0][c][i];
+  for (int j = 0; j < kGradVerts; ++j) {
+    const int i = threadIdx.x + j * kGradThreads;
+    if (i >= nv) continue;
+    V4<R> q4 = acc4[i];
+    V2<R> q2 = acc2[i];
 #pragma unroll
-      for (int w = 1; w < kGradWarps; ++w) s += acc[w][c][i];
-      q[c] = s;
+    for (int w = 1; w < kGradWarps; ++w) {
+      const V4<R> r4 = acc4[w * kTileVerts + i];
+      const V2<R> r2 = acc2[w * kTileVerts + i];
+      q4.x += r4.x;
+      q4.y += r4.y;
+      q4.z += r4.z;
+      q4.w += r4.w;
+      q2.x += r2.x;
+      q2.y += r2.y;
     }
-    const int sidx = a.slot_of_tv[vs + i];
-    slots[sidx] = V4<R>{q[0], q[1], q[2], R(0)};
-    slots[(size_t)a.n_slots + sidx] = V4<R>{q[3], q[4], q[5], R(0)};
+    slots[2 * sidx[j]] = V4<R>{q4.x, q4.y, q4.z, R(0)};
+    slots[2 * sidx[j] + 1] = V4<R>{q4.w, q2.x, q2.y, R(0)};
   }
   block_reduce<1, 0x0u, R>(sums, red);
   if (threadIdx.x == 0) ((AccStore<R>*)a.part_b)[blockIdx.x] = acc_store(sums[0]);
@@ -473,7 +555,7 @@ __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 
 // vertex pass
 // ---------------------------------------------------------------------------
 template <class R>
-__global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, int use_cond) {
+__global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_kernel(SolveArgs a, int use_cond) {
   constexpr int N = 12;
   __shared__ Acc<R> red[(kVThreads / 32) * N];
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -490,32 +572,30 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
       cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
     return;
   }
-  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean, t = (R)st->t;
-  V4<R>* X = (V4<R>*)a.x;
-  V4<R>* XL = (V4<R>*)a.xlo;
-  V4<R>* Gv = (V4<R>*)a.g;
-  V4<R>* Dv = (V4<R>*)a.d;
-  V4<R>* PO = (V4<R>*)a.po;
+  const R t = (R)st->t;
+  V4<R>* XA = (V4<R>*)a.xa;
+  V4<R>* GD = (V4<R>*)a.gd;
+  const V4<R>* P = p_cur<R>(a, st->pbuf);
   const V4<R>* F = (const V4<R>*)a.force;
   const V4<R>* slots = (const V4<R>*)a.slots;
   // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
-  Acc<R> s[N] = {};
+  // a thread sums its few vertices in R; float-float starts at the warp trees
+  R s[N] = {};
   for (int i = i0; i < a.n_points; i += gridDim.x * blockDim.x) {
     if (i != i0) {
       s0 = a.off[i];
       s1 = a.off[i + 1];
     }
-    const V4<R> x = X[i], xl = XL[i], g = Gv[i], d = Dv[i], po = PO[i];
+    const V4<R> x = XA[2 * i], xl = XA[2 * i + 1], g = GD[2 * i], pv = ldg4(P + i);
     const int mask = (int)x.w;
-    R p[3];
-    pdir(g, d, po, beta, inv_mean, p);
+    const R p[3] = {pv.x, pv.y, pv.z};
     R xh[3] = {x.x, x.y, x.z}, xlo[3] = {xl.x, xl.y, xl.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c) pair_add(xh[c], xlo[c], mul_rn(t, p[c]));
     const R xn[3] = {xh[0] + xlo[0], xh[1] + xlo[1], xh[2] + xlo[2]};
     R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
     for (int k = s0; k < s1; ++k) {
-      const V4<R> sg = slots[k], sd = slots[(size_t)a.n_slots + k];
+      const V4<R> sg = slots[2 * k], sd = slots[2 * k + 1];
       gs[0] += sg.x;
       gs[1] += sg.y;
       gs[2] += sg.z;
@@ -528,7 +608,7 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
       gs[0] -= f.x;
       gs[1] -= f.y;
       gs[2] -= f.z;
-      s[11].add(-(f.x * xn[0] + f.y * xn[1] + f.z * xn[2]));
+      s[11] += -(f.x * xn[0] + f.y * xn[1] + f.z * xn[2]);
     }
     const R go[3] = {g.x, g.y, g.z};
     R gn[3], dn[3];
@@ -542,30 +622,35 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
       const R ad = fabs(dn[c]);
       if (ad > R(0)) {
         const R P = rcp_rn(ad);
-        s[0].add(gn[c] * gn[c] * P);
-        s[1].add(gn[c] * y * P);
-        s[2].add(y * y * P);
-        s[3].add(ad);
-        s[4].add(R(1));
+        s[0] += gn[c] * gn[c] * P;
+        s[1] += gn[c] * y * P;
+        s[2] += y * y * P;
+        s[3] += ad;
+        s[4] += R(1);
       } else {
-        s[5].add(gn[c] * gn[c]);
-        s[6].add(gn[c] * y);
-        s[7].add(y * y);
+        s[5] += gn[c] * gn[c];
+        s[6] += gn[c] * y;
+        s[7] += y * y;
       }
-      s[8].add(y * p[c]);
-      s[9].add(p[c] * gn[c]);
-      s[10].add(gn[c] * gn[c]);
+      s[8] += y * p[c];
+      s[9] += p[c] * gn[c];
+      s[10] += gn[c] * gn[c];
     }
-    X[i] = V4<R>{xh[0], xh[1], xh[2], x.w};
-    XL[i] = V4<R>{xlo[0], xlo[1], xlo[2], R(0)};
-    Gv[i] = V4<R>{gn[0], gn[1], gn[2], R(0)};
-    Dv[i] = V4<R>{dn[0], dn[1], dn[2], R(0)};
-    PO[i] = V4<R>{p[0], p[1], p[2], R(0)};
+    XA[2 * i] = V4<R>{xh[0], xh[1], xh[2], x.w};
+    XA[2 * i + 1] = V4<R>{xlo[0], xlo[1], xlo[2], R(0)};
+    GD[2 * i] = V4<R>{gn[0], gn[1], gn[2], R(0)};
+    GD[2 * i + 1] = V4<R>{dn[0], dn[1], dn[2], R(0)};
   }
   double tot[N];
-  // float-float warp trees for the sums whose terms change sign
+  // float-float block sums for the quantities whose terms change sign
   constexpr unsigned FF = (1u << 1) | (1u << 6) | (1u << 8) | (1u << 9);
-  if (!grid_reduce_masked<N, FF, R>(s, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
+  Acc<R> acc[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    acc[k] = Acc<R>{};
+    acc[k].add(s[k]);
+  }
+  if (!grid_reduce_masked<N, FF, R>(acc, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
   if (threadIdx.x != 0) return;
   const double cnt = tot[4], sad = tot[3];
   const double inv_m = (cnt > 0.0 && sad > 0.0) ? cnt / sad : 1.0;
@@ -587,6 +672,7 @@ __global__ void __launch_bounds__(kVThreads) solver_vertex_kernel(SolveArgs a, i
   }
   st->beta = b;
   st->inv_mean = inv_m;
+  st->pbuf ^= 1;  // this iteration's p becomes p_prev
   st->gd = gd;
   st->gnorm = gnorm;
   st->ext_energy = tot[11];
@@ -637,11 +723,13 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     if (mask & 1) x.x = fx.x;
     if (mask & 2) x.y = fx.y;
     if (mask & 4) x.z = fx.z;
-    ((V4<R>*)a.x)[i] = x;
-    ((V4<R>*)a.xlo)[i] = V4<R>{R(0), R(0), R(0), R(0)};
-    ((V4<R>*)a.g)[i] = V4<R>{R(0), R(0), R(0), R(0)};
-    ((V4<R>*)a.d)[i] = V4<R>{R(0), R(0), R(0), R(0)};
-    ((V4<R>*)a.po)[i] = V4<R>{R(0), R(0), R(0), R(0)};
+    const V4<R> z{R(0), R(0), R(0), R(0)};
+    ((V4<R>*)a.xa)[2 * i] = x;
+    ((V4<R>*)a.xa)[2 * i + 1] = z;
+    ((V4<R>*)a.gd)[2 * i] = z;
+    ((V4<R>*)a.gd)[2 * i + 1] = z;
+    ((V4<R>*)a.p0)[i] = z;
+    ((V4<R>*)a.p1)[i] = z;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     SolverState* st = a.st;
@@ -667,41 +755,35 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     st->ls_ok = 0;
     st->decided = 1;
     st->error = 0;
+    st->pbuf = 0;
   }
 }
 
 __global__ void solver_set_limit_kernel(SolverState* st, int n) { st->iter_limit = st->iter + n; }
 
 template <class R>
-__global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ x, const V4<R>* __restrict__ xlo,
-                                     const int32_t* __restrict__ uoi, R* __restrict__ u) {
+__global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ xa, const int32_t* __restrict__ uoi,
+                                     R* __restrict__ u) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const size_t k = 3 * (size_t)uoi[i];
-    const V4<R> v = x[i], l = xlo[i];
+    const V4<R> v = xa[2 * i], l = xa[2 * i + 1];
     u[k] = v.x + l.x;
     u[k + 1] = v.y + l.y;
     u[k + 2] = v.z + l.z;
   }
 }
 
-cudaError_t solver_prepare_kernels(int precision) {
-  cudaError_t e;
-  if (precision == AGB_F64) {
-    const int bytes = (int)grad_smem_bytes<double>();
-    e = cudaFuncSetAttribute(solver_grad_kernel<double, AGB_ARAP>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(solver_grad_kernel<double, AGB_STABLE_NEO_HOOKEAN>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  } else {
-    const int bytes = (int)grad_smem_bytes<float>();
-    e = cudaFuncSetAttribute(solver_grad_kernel<float, AGB_ARAP>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(solver_grad_kernel<float, AGB_STABLE_NEO_HOOKEAN>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  }
+template <class R>
+static cudaError_t prepare_t() {
+  const int g = (int)grad_smem_bytes<R>();
+  const cudaFuncAttribute m = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_ARAP>, m, g);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN>, m, g);
   return e;
+}
+
+cudaError_t solver_prepare_kernels(int precision) {
+  return precision == AGB_F64 ? prepare_t<double>() : prepare_t<float>();
 }
 
 cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,
@@ -811,11 +893,11 @@ cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_
                                    cudaStream_t s) {
   const int blocks = solver_vertex_blocks(a.n_points);
   if (a.precision == AGB_F64)
-    solver_unpack_kernel<double><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<double>*)a.x,
-                                                             (const V4<double>*)a.xlo, uoi, (double*)u);
+    solver_unpack_kernel<double><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<double>*)a.xa, uoi,
+                                                             (double*)u);
   else
-    solver_unpack_kernel<float><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<float>*)a.x,
-                                                            (const V4<float>*)a.xlo, uoi, (float*)u);
+    solver_unpack_kernel<float><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<float>*)a.xa, uoi,
+                                                            (float*)u);
   return cudaGetLastError();
 }
 

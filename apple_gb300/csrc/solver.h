@@ -40,6 +40,7 @@ struct SolverState {
   int32_t ls_ok;
   int32_t decided;     // ARAP: a trial pass has decided the step
   int32_t error;       // device-side status (nonzero = a guard tripped)
+  int32_t pbuf;        // p[pbuf] holds p_prev; the direction pass writes p into p[pbuf ^ 1]
 };
 
 // Everything a solver kernel needs, by value.
@@ -47,15 +48,18 @@ struct SolveArgs {
   FemView fv;
   int n_points;
   int precision;
-  void* x;     // V4<R> n_points: position hi part, w = fixed mask bits
-  void* xlo;   // V4<R> n_points: position lo part (x = hi + lo)
-  void* g;     // V4<R> free gradient (fixed components 0)
-  void* d;     // V4<R> Hessian diagonal (fixed components 0)
-  void* po;    // V4<R> previous direction
+  // Vertex state, per internal vertex v (V4<R> = 4 lanes of R):
+  //   xa[2v] = (x_hi, fixed-mask bits), xa[2v+1] = (x_lo, 0); x = hi + lo
+  //   gd[2v] = (g, 0) free gradient, gd[2v+1] = (d, 0) Hessian diagonal
+  //   p0[v], p1[v]: search directions; p[pbuf] = p_prev, p[pbuf ^ 1] = p
+  void* xa;
+  void* gd;
+  void* p0;
+  void* p1;
   const void* force;  // V4<R> external force per vertex or null
   const int32_t* slot_of_tv;
   const int32_t* off;  // CSR over slots (n_points + 1)
-  void* slots;         // V4<R> [2][n_slots]
+  void* slots;         // V4<R> [n_slots][2]: (gradient, 0), (diagonal, 0)
   int32_t n_slots;
   SolverState* st;
   void* part_a;        // direction-pass partials (n_tiles x 6) and group partials
@@ -110,11 +114,10 @@ struct agb_solver {
   void* d_rec = nullptr;
   uint32_t* d_ids = nullptr;
   // vertex state
-  void* d_x = nullptr;
-  void* d_xlo = nullptr;
-  void* d_g = nullptr;
-  void* d_d = nullptr;
-  void* d_po = nullptr;
+  void* d_xa = nullptr;
+  void* d_gd = nullptr;
+  void* d_p0 = nullptr;
+  void* d_p1 = nullptr;
   void* d_slots = nullptr;
   void* d_part = nullptr;
   unsigned* d_cnt = nullptr;

@@ -19,6 +19,11 @@ struct alignas(4 * sizeof(R)) V4 {
 };
 
 template <class R>
+struct alignas(2 * sizeof(R)) V2 {
+  R x, y;
+};
+
+template <class R>
 __device__ __forceinline__ V4<R> ldg4(const V4<R>* p);
 template <>
 __device__ __forceinline__ V4<float> ldg4<float>(const V4<float>* p) {

@@ -55,6 +55,8 @@ def _args():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
+    ap.add_argument("--profile", action="store_true",
+                    help="run warmup iterations, then each pass `steps` times as plain launches (ncu captures)")
     return ap.parse_args()
 
 
@@ -118,18 +120,19 @@ class ClockSampler:
 
 
 def _dist():
+    """(world, rank, local) from the torchrun environment; NCCL across GPUs, gloo without CUDA."""
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    cuda = torch.cuda.is_available()
+    if cuda:
+        torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if cuda else "gloo")
     return world, rank, local
 
 
@@ -146,9 +149,16 @@ def _max_over_ranks(world, x: float) -> float:
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def _aggregate(world, units_per_rank: float, local_seconds: float):
+    """Whole-job throughput: all ranks' units over the slowest rank's time."""
+    total_s = _max_over_ranks(world, local_seconds)
+    return world * units_per_rank / total_s, total_s
 
 
 def cpu_reference(steps_req: int, budget: float, small: bool = False) -> dict:
@@ -227,6 +237,17 @@ def run_ours(a) -> None:
         flush.fill_(i & 0xFF)
         solver.step()
     torch.cuda.synchronize(dev)
+    if a.profile:
+        # the three passes as plain launches (graph nodes that set a
+        # conditional handle cannot be profiled individually), inside an
+        # NVTX range for ncu's --nvtx-include "profile/"
+        ms = (ctypes.c_float * 3)()
+        torch.cuda.nvtx.range_push("profile")
+        _lib.call("agb_solver_time_passes", solver.handle, a.steps, ctypes.c_void_p(flush.data_ptr()),
+                  flush.numel(), ms, stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        torch.cuda.nvtx.range_pop()
+        return
     clocks = ClockSampler(local)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
     _barrier(world)
@@ -240,11 +261,10 @@ def run_ours(a) -> None:
     _barrier(world)
     clk = clocks.stop()
     step_ms = [s.elapsed_time(e) for s, e in ev]
-    total_s = _max_over_ranks(world, sum(step_ms) / 1e3)
+    value, total_s = _aggregate(world, a.steps, sum(step_ms) / 1e3)
     state = solver.read()
     if state.result != ag.Result.UNKNOWN_ERROR:
         raise RuntimeError(f"solver stopped inside the timed region: {state}")
-    value = world * a.steps / total_s
     b_iter = nt * B_TET + nv * B_VERT
 
     # each pass alone, L2 flushed before each launch
@@ -282,8 +302,8 @@ def run_ours(a) -> None:
             times.append(t1 - t0)
         if sol.n_steps != a.e2e_iters:
             raise RuntimeError(f"e2e solve ran {sol.n_steps} iterations")
-    e2e_s = _max_over_ranks(world, statistics.mean(times))
-    e2e = {"value": world * a.e2e_iters / e2e_s, "unit": "iter/s",
+    e2e_value, e2e_s = _aggregate(world, a.e2e_iters, statistics.mean(times))
+    e2e = {"value": e2e_value, "unit": "iter/s",
            "h2d_bytes_per_step": nv * 3 * 4, "d2h_bytes_per_step": nv * 3 * 4 + 160,
            "iters_per_step": a.e2e_iters, "ms_per_step": e2e_s * 1e3}
 

@@ -25,6 +25,10 @@
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
+
+/* loops shorter than this run on one thread: small cases are then
+ * deterministic (no atomic or reduction-order effects) */
+#define ORC_PAR_MIN 4096
 #endif
 
 #define ORC_FUN 1u
@@ -285,7 +289,7 @@ int orc_eval(int material, int n_points, int n_cells, const int32_t* cells, cons
              double* grad, double* diag, double* prod, double* quad) {
   orc_fem m = {material, n_points, n_cells, cells, dhdX, dV, mu, lam};
   double e_sum = 0.0, q_sum = 0.0;
-#pragma omp parallel for schedule(static) reduction(+ : e_sum, q_sum)
+#pragma omp parallel for schedule(static) reduction(+ : e_sum, q_sum) if (n_cells >= ORC_PAR_MIN)
   for (int e = 0; e < n_cells; ++e) {
     double uc[4][3], D[4][3], F[3][3], out[4][3];
     load(&m, e, u, uc, D);
@@ -347,7 +351,7 @@ typedef struct {
 
 static double dot_masked(int n3, const double* a, const double* b, const uint8_t* mask) {
   double s = 0;
-#pragma omp parallel for reduction(+ : s)
+#pragma omp parallel for reduction(+ : s) if (n3 >= ORC_PAR_MIN)
   for (int i = 0; i < n3; ++i)
     if (!mask[i]) s += a[i] * b[i];
   return s;
@@ -360,7 +364,7 @@ static double model_fun(const orc_fem* m, const double* u, const double* force) 
   if (force) {
     double w = 0;
     int n3 = 3 * m->n_points;
-#pragma omp parallel for reduction(+ : w)
+#pragma omp parallel for reduction(+ : w) if (n3 >= ORC_PAR_MIN)
     for (int i = 0; i < n3; ++i) w -= force[i] * u[i];
     e += w;
   }
