@@ -46,6 +46,14 @@ class PncgStats(ctypes.Structure):
     ]
 
 
+class CgParams(ctypes.Structure):
+    _fields_ = [("max_iter", c_int32), ("rtol", c_double), ("atol", c_double)]
+
+
+class CgStats(ctypes.Structure):
+    _fields_ = [("result", c_int32), ("n_iter", c_int32), ("residual", c_double), ("residual_first", c_double)]
+
+
 class AgbError(RuntimeError):
     """A non-zero status from the C ABI."""
 
@@ -92,6 +100,9 @@ _SIGNATURES = {
     "agb_solver_read": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_pncg_minimize_host": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_solver_time_passes": (c_int, [c_void_p, c_int32, c_void_p, ctypes.c_size_t, POINTER(ctypes.c_float), c_void_p]),
+    "agb_cg_default_params": (None, [POINTER(CgParams)]),
+    "agb_solver_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(CgParams), POINTER(CgStats), c_void_p]),
+    "agb_fem_grad_param_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

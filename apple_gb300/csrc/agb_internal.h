@@ -129,6 +129,9 @@ struct agb_fem {
   int32_t* d_own_off = nullptr;   // n_points + 1
   void* d_rec = nullptr;
   uint32_t* d_ids = nullptr;
+  std::vector<double> vol_internal;  // dV * fraction per internal element
+  int32_t* d_elem_user = nullptr;    // internal -> caller's cell index (on first use)
+  void* d_vol = nullptr;             // R per internal element (on first use)
   // scratch for the standalone evaluation API
   void* d_u = nullptr;      // V4<R> n_points
   void* d_p = nullptr;      // V4<R> n_points

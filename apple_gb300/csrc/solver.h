@@ -96,6 +96,51 @@ size_t solver_grad_smem(int precision);
 // one pass of an iteration on its own: 0 direction, 1 gradient, 2 vertex
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s);
 
+// Adjoint CG (adjoint.cu): scalars of H lam = rhs on the free DOFs at the
+// solver's current x, kept on the device like SolverState.
+struct CgState {
+  double alpha, beta;
+  double rz;   // r . M^-1 r
+  double rr;   // r . r
+  double rr0;  // r . r at the start
+  double rtol, atol;
+  int32_t max_iter;
+  int32_t iter;
+  int32_t iter_limit;
+  int32_t done;
+  int32_t result;
+  int32_t pbuf;  // p[pbuf] = p_prev, p[pbuf ^ 1] = p
+};
+
+struct CgArgs {
+  SolveArgs a;  // mesh, tiles, slots, positions x = hi + lo (read only)
+  void* lam;    // V4<R> solution
+  void* res;    // V4<R> residual
+  void* q;      // V4<R> H p
+  void* minv;   // V4<R> Jacobi M^-1 (0 on fixed components)
+  void* p0;
+  void* p1;
+  void* part;   // reduction partials (vblocks x 2)
+  unsigned* cnt;
+  CgState* cs;
+  int vblocks;
+  unsigned long long cond;
+};
+
+cudaError_t cg_prepare_kernels(int precision);
+size_t cg_smem(int precision);
+cudaError_t launch_cg_init(const CgArgs& c, const void* rhs_user, const int32_t* user_of_internal,
+                           cudaStream_t s);
+// one CG iteration: element pass (H p), two vertex passes
+cudaError_t launch_cg_iteration(const CgArgs& c, cudaStream_t s);
+cudaError_t launch_cg_set_limit(const CgArgs& c, int n, cudaStream_t s);
+cudaError_t launch_cg_unpack(const CgArgs& c, const int32_t* user_of_internal, void* out_user,
+                             cudaStream_t s);
+// out_mu[c] += d(w . grad)/d mu_c (and lambda), cells in the caller's order
+cudaError_t launch_param_vjp(const FemView& fv, int precision, const void* u_int, const void* w_int,
+                             const void* vol, const int32_t* elem_user, void* out_mu, void* out_lam,
+                             cudaStream_t s);
+
 }  // namespace agb
 
 struct agb_solver {
@@ -125,6 +170,14 @@ struct agb_solver {
   agb::SolverState* h_state = nullptr;  // pinned
   void* d_u_tmp = nullptr;              // caller-order staging for host I/O
   agb::SolveArgs args{};
+  // adjoint CG (allocated on first use)
+  void* d_cg = nullptr;            // lam, res, q, minv, p0, p1: 6 x V4<R> x n_points
+  void* d_cg_part = nullptr;
+  unsigned* d_cg_cnt = nullptr;
+  agb::CgState* d_cg_state = nullptr;
+  agb::CgState* h_cg_state = nullptr;  // pinned
+  agb::CgArgs cg{};
+  cudaGraphExec_t cg_exec = nullptr;
   // graphs
   cudaGraphExec_t loop_exec = nullptr;
   cudaGraphExec_t step_exec = nullptr;

@@ -223,6 +223,22 @@ class WarpPotentialFem:
         check_scalar(output, "output")
         _lib.call("agb_fem_hess_quad", self._standalone(), ptr(u), ptr(p), ptr(output), stream_ptr(u.device))
 
+    def grad_param_vjp(self, u: torch.Tensor, w: torch.Tensor) -> dict:
+        """Backward of ``grad`` on the cell materials: ``{"mu": d(w.grad(u))/d mu,
+        "lambda": d(w.grad(u))/d lambda}`` per cell (what Warp's tape gives for the
+        arrays in ``requires_grad``, warp/fem/_base.py:80-117)."""
+        check_vec(u, self.n_points, self.dtype, "u")
+        w = check_vec(w.to(self.dtype), self.n_points, self.dtype, "w")
+        n = self.cells.shape[0]
+        dmu = torch.zeros(n, dtype=self.dtype, device=u.device)
+        dlam = torch.zeros(n, dtype=self.dtype, device=u.device)
+        _lib.call("agb_fem_grad_param_vjp", self._standalone(), ptr(u), ptr(w), ptr(dmu), ptr(dlam),
+                  stream_ptr(u.device))
+        out = {"mu": dmu}
+        if self.material == _lib.STABLE_NEO_HOOKEAN:
+            out["lambda"] = dlam
+        return out
+
     def eval(self, u: torch.Tensor, p: torch.Tensor | None = None, *, fun=False, grad=False,
              hess_diag=False, hess_prod=False, hess_quad=False) -> dict:
         """Fused: the requested quantities from one pass over the mesh (new tensors)."""

@@ -94,6 +94,18 @@ class OptState:
     result: Result
 
 
+@dataclasses.dataclass(frozen=True)
+class CgSolution:
+    result: Result
+    n_iter: int
+    residual: float
+    residual_first: float
+
+    @property
+    def success(self) -> bool:
+        return self.result == Result.PRIMARY_SUCCESS
+
+
 class DeviceSolver:
     """One ``agb_solver`` bound to a device model."""
 
@@ -125,6 +137,18 @@ class DeviceSolver:
         _lib.call("agb_solver_read", self.handle, ptr(u_out), ctypes.byref(st), stream_ptr())
         return Solution(Result(st.result), st.n_steps, st.grad_norm, st.grad_norm_first, st.energy, st.alpha,
                         st.beta, st.line_search_steps, bool(st.line_search_ok))
+
+    def adjoint(self, rhs: torch.Tensor, *, rtol: float = 1e-6, atol: float = 0.0,
+                max_iter: int = 10000) -> tuple[torch.Tensor, "CgSolution"]:
+        """Solve H(u*) lam = rhs on the free DOFs at the solver's current state
+        (``agb_solver_adjoint``); lam is 0 on fixed components."""
+        rhs = rhs.to(self.warp_model.dtype).contiguous()
+        lam = torch.empty_like(rhs)
+        prm = _lib.CgParams(int(max_iter), float(rtol), float(atol))
+        st = _lib.CgStats()
+        _lib.call("agb_solver_adjoint", self.handle, ptr(rhs), ptr(lam), ctypes.byref(prm), ctypes.byref(st),
+                  stream_ptr(rhs.device))
+        return lam, CgSolution(Result(st.result), st.n_iter, st.residual, st.residual_first)
 
     def minimize_host(self, u_host: torch.Tensor) -> Solution:
         """Solve from a HOST (CPU) tensor, in place (``agb_pncg_minimize_host``)."""

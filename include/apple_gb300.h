@@ -207,6 +207,50 @@ int agb_solver_time_passes(agb_solver* solver, int32_t reps, void* flush, size_t
  * in, solves to termination, copies the result back into u_host. */
 int agb_pncg_minimize_host(agb_solver* solver, void* u_host, agb_pncg_stats* stats, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Differentiation of the converged equilibrium g(u*, theta) = 0 (the inverse
+ * experiments' adjoint, exp/2025/09/24/inverse-grin/src/32-inverse.py:223-300):
+ * dL/dtheta = -lam^T dg/dtheta with H(u*) lam = dL/du on the free DOFs.
+ * ------------------------------------------------------------------------- */
+typedef struct agb_cg_params {
+  int32_t max_iter;            /* 10000 */
+  double rtol;                 /* ||r|| <= max(atol, rtol ||r_0||); 1e-6 */
+  double atol;                 /* 0 */
+} agb_cg_params;
+
+typedef struct agb_cg_stats {
+  int32_t result;              /* AGB_PRIMARY_SUCCESS, AGB_MAX_STEPS_REACHED, AGB_NAN_ENCOUNTERED,
+                                  AGB_LINE_SEARCH_FAILED (p^T H p <= 0: H not positive definite) */
+  int32_t n_iter;
+  double residual;             /* ||r|| at the end (free DOFs) */
+  double residual_first;       /* ||r_0|| = ||rhs|| on the free DOFs */
+} agb_cg_stats;
+
+void agb_cg_default_params(agb_cg_params* params);
+
+/* Solve H(x) lam = rhs on the free DOFs at the solver's current x (after
+ * agb_solver_iterate: the converged u*) with Jacobi-preconditioned CG
+ * (jax.scipy.sparse.linalg.cg with M = 1/hess_diag in the reference recipe;
+ * M from the Hessian diagonal at x, zero entries replaced by the mean of the
+ * positive ones as in the PNCG preconditioner).  H is the sum of the model's
+ * hess_prod (warp/fem/_base.py:326-351); fixed components of lam are 0.
+ * rhs and lam: device, caller order, n_points x 3 of the solver precision.
+ * The CG loop runs on the device as one CUDA graph launch; stats on the host.
+ * The solver's PNCG state is not modified.  Only for models whose potentials
+ * share one material (the solver's element passes). */
+int agb_solver_adjoint(agb_solver* solver, const void* rhs, void* lam, const agb_cg_params* params,
+                       agb_cg_stats* stats, void* stream);
+
+/* Backward of the gradient on the cell materials (the Warp tape over the
+ * arrays marked requires_grad, warp/fem/_base.py:80-117,
+ * utils/_material.py:34-38): for a vector field w (device, caller order,
+ * n_points x 3) and displacement u,
+ *   out_mu[c]     += d(w . grad(u))/d mu_c
+ *   out_lambda[c] += d(w . grad(u))/d lambda_c   (stable Neo-Hookean; may be NULL)
+ * with cells in the caller's order (device arrays of the fem's precision). */
+int agb_fem_grad_param_vjp(agb_fem* fem, const void* u, const void* w, void* out_mu, void* out_lambda,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

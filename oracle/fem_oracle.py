@@ -414,6 +414,23 @@ class FemPotential:
         """Sum_e max(dV p^T H_e p, 0)  (``_base.py:353-383``)."""
         return float(np.sum(self.hess_quad_elems(u, p)))
 
+    def grad_param_vjp(self, u, w):
+        """d(w . grad(u))/d mu_c and d/d lambda_c per cell: the backward of the
+        grad kernel on the material arrays (``_base.py:80-117`` with Warp's tape;
+        ``utils/_material.py:34-38``).  grad is linear in mu and lambda:
+        SNH P = mu (F - cof F) + lambda (J-1) cof F  (``_stable_neo_hookean.py:30-39``),
+        ARAP P = mu (F - R)  (``_arap.py:24-28``)."""
+        F = self._F(u)
+        W = deformation_gradient_jvp(self.dhdX, w[self.cells])  # sum_a w_a (x) dhdX_a
+        if self.material == Material.ARAP:
+            R, _ = polar_rv(F)
+            return ddot(F - R, W) * self.dV, None
+        C = g3(F)
+        J = I3(F)
+        dmu = ddot(F - C, W) * self.dV
+        dlam = (J - 1.0) * ddot(C, W) * self.dV
+        return dmu, dlam
+
 
 @dataclasses.dataclass
 class ExternalForce:
@@ -661,6 +678,34 @@ def solve_model(model: Model, u0_full: np.ndarray | None = None, **kw):
     hq = lambda x, p: model.hess_quad(dm.to_full(x), dm.to_full_grad(p))  # noqa: E731
     x, stats = pncg_minimize(fun, grad, hd, hq, x0, **kw)
     return dm.to_full(x), stats
+
+
+def dense_hessian_free(model: Model, u: np.ndarray) -> np.ndarray:
+    """H(u) on the free DOFs, column by column from hess_prod (small meshes)."""
+    dm = model.dof_map
+    free = dm.free_indices
+    H = np.empty((free.size, free.size))
+    for j, k in enumerate(free):
+        e = np.zeros(u.size)
+        e[k] = 1.0
+        H[:, j] = model.hess_prod(u, e.reshape(-1, 3)).reshape(-1)[free]
+    return 0.5 * (H + H.T)
+
+
+def adjoint_dense(model: Model, u: np.ndarray, rhs: np.ndarray) -> np.ndarray:
+    """lam with H(u) lam = rhs on the free DOFs (0 on fixed), by a dense solve."""
+    dm = model.dof_map
+    lam_free = np.linalg.solve(dense_hessian_free(model, u), rhs.reshape(-1)[dm.free_indices])
+    return dm.to_full_grad(lam_free)
+
+
+def equilibrium_param_grad(model: Model, potential: FemPotential, u: np.ndarray, dLdu: np.ndarray):
+    """Implicit differentiation of g(u*, theta) = 0 (the reference's inverse
+    recipe, ``exp/2025/09/24/inverse-grin/src/32-inverse.py:223-300``):
+    dL/dmu, dL/dlambda = -d(lam . g)/d(mu, lambda), H lam = dL/du."""
+    lam = adjoint_dense(model, u, dLdu)
+    dmu, dlam = potential.grad_param_vjp(u, lam)
+    return -dmu, (None if dlam is None else -dlam), lam
 
 
 # ---------------------------------------------------------------------------
