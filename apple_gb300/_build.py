@@ -24,7 +24,7 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", f"-I{CUDA_HOME}/include"]
 
-CU_SOURCES = ["fem_eval.cu", "solver.cu", "fem_noalloc.cu", "adjoint.cu"]
+CU_SOURCES = ["fem_eval.cu", "solver.cu", "fem_noalloc.cu", "adjoint.cu", "batch.cu"]
 CXX_SOURCES = ["capi.cpp", "prep.cpp"]
 
 

@@ -100,6 +100,13 @@ _SIGNATURES = {
     "agb_solver_read": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_pncg_minimize_host": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_solver_time_passes": (c_int, [c_void_p, c_int32, c_void_p, ctypes.c_size_t, POINTER(ctypes.c_float), c_void_p]),
+    "agb_batch_create": (c_int, [c_int32, c_void_p, POINTER(PncgParams), c_int32, POINTER(c_void_p)]),
+    "agb_batch_destroy": (c_int, [c_void_p]),
+    "agb_batch_info": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
+    "agb_batch_reset": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "agb_batch_iterate": (c_int, [c_void_p, c_int32, c_void_p]),
+    "agb_batch_step": (c_int, [c_void_p, c_void_p]),
+    "agb_batch_read": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_cg_default_params": (None, [POINTER(CgParams)]),
     "agb_solver_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(CgParams), POINTER(CgStats), c_void_p]),
     "agb_fem_grad_param_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

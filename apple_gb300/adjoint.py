@@ -18,6 +18,7 @@ whose per-cell ``mu`` (and ``lambda``) are the parameters, and
 from __future__ import annotations
 
 import dataclasses
+import time
 
 import numpy as np
 import torch
@@ -63,6 +64,7 @@ class MaterialEquilibrium:
         self.device = torch.device(device)
         self._state = None  # (potential, solver, u*) of the last forward
         self.stats: AdjointStats | None = None
+        self.timings: dict[str, float] = {}  # seconds of the last solve() / vjp() phases
 
     @property
     def n_cells(self) -> int:
@@ -70,6 +72,7 @@ class MaterialEquilibrium:
 
     def solve(self, mu, lam=None) -> torch.Tensor:
         """Forward: the converged displacement (n_points, 3) for these cell materials."""
+        t0 = time.perf_counter()
         mesh = meshgen.TetMesh(self.points, self.cells)
         mesh.cell_data[MU] = np.asarray(torch.as_tensor(mu).detach().cpu(), np.float64)
         if lam is not None:
@@ -89,10 +92,16 @@ class MaterialEquilibrium:
         model = b.finalize()
         opt = PNCG(self.criteria)
         fwd = Forward(model, opt)
+        opt.solver(fwd.problem)  # device set-up outside the timed solve
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
         sol = fwd.step()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
         u = fwd.state.u
         self._state = (pot, opt.solver(fwd.problem), u, model)
         self.stats = AdjointStats(sol)
+        self.timings = {"build": t1 - t0, "forward": t2 - t1}
         return u
 
     def vjp(self, grad_u: torch.Tensor) -> dict:
@@ -100,12 +109,16 @@ class MaterialEquilibrium:
         if self._state is None:
             raise RuntimeError("call solve() first")
         pot, sv, u, _ = self._state
-        lam, cg = sv.adjoint(grad_u.to(self.dtype).to(u.device).contiguous(), rtol=self.cg_rtol,
-                             max_iter=self.cg_max_iter)
+        rhs = grad_u.to(self.dtype).to(u.device).contiguous()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lam, cg = sv.adjoint(rhs, rtol=self.cg_rtol, max_iter=self.cg_max_iter)
         self.stats = dataclasses.replace(self.stats, cg=cg)
         if cg.result not in (Result.PRIMARY_SUCCESS,):
             raise RuntimeError(f"adjoint CG did not converge: {cg}")
         out = pot.grad_param_vjp(u, lam)
+        torch.cuda.synchronize()
+        self.timings["adjoint"] = time.perf_counter() - t0
         return {k: -v for k, v in out.items()}
 
 

@@ -1,0 +1,311 @@
+// Batched PNCG: many independent meshes, one set of launches per iteration.
+//
+// The meshes' vertices and tiles are concatenated (tiles never span meshes,
+// vertex chunks never span meshes).  An iteration is five kernels, captured
+// once in a CUDA graph; every mesh carries its own SolverState, so each one
+// runs the reference's PNCG iteration (benches/bench_pncg_branching_backends.py
+// :254-456, 606-679) with its own beta, step and termination:
+//   direction pass   one CTA per tile: p of the tile's mesh, p^T H p and the
+//                    energy polynomial; one partial per tile
+//   direction tail   one CTA per mesh: the mesh's tile partials in tile order,
+//                    then the Armijo decision (dir_decide)
+//   gradient pass    one CTA per tile at x + t_mesh p (grad_tile)
+//   vertex pass      one CTA per vertex chunk: x, g, d and the 12 sums
+//   vertex tail      one CTA per mesh: chunk partials in order, then beta and
+//                    termination (vertex_decide); the last CTA to finish
+//                    counts the meshes still running and sets the graph's
+//                    while-condition
+// Tiles and chunks of a finished mesh return at once.
+#include "kernels.h"
+#include "solver.h"
+#include "solver_common.cuh"
+
+namespace agb {
+
+namespace {
+
+constexpr int kTailThreads = 256;
+
+template <class R>
+__global__ void __launch_bounds__(kElemThreads) batch_dir_kernel(BatchArgs b) {
+  constexpr int N = 6;
+  constexpr unsigned FF = 0x2u;  // float-float warp tree for c2 (terms of both signs)
+  __shared__ V4<R> sx[kTileVerts];
+  __shared__ V4<R> sp[kTileVerts];
+  __shared__ Acc<R> red[kWarps * N];
+  const SolveArgs& a = b.a;
+  const int tile = blockIdx.x;
+  if (b.cond && tile == 0 && threadIdx.x == 0)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)b.cond, 0u);  // the vertex tail re-arms
+  pdl_trigger();
+  SolverState* st = b.st + b.tile_mesh[tile];
+  if (st->done) return;
+  const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
+  const int pb = st->pbuf;
+  stage_dir<R>(a, tile_vertex(a.fv, tile, threadIdx.x), beta, inv_mean, p_prev<R>(a, pb), p_cur<R>(a, pb), sx,
+               sp);
+  __syncthreads();
+  Acc<R> sums[N] = {};
+  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem<R>(a.fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R G[3][3], dF[3][3];
+    vec_gradient(sx, l, geo.D, G);
+    vec_gradient(sp, l, geo.D, dF);
+    SnhPoint<R> s;
+    snh_prepare(G, s);
+    SnhDir<R> d;
+    snh_dir(s, dF, d);
+    sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
+    R c[5];
+    snh_poly(s, d, geo.mu, geo.lam, c);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
+  }
+  block_reduce<N, FF, R>(sums, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) ((AccStore<R>*)b.part_dir)[(size_t)tile * N + k] = acc_store(sums[k]);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs b) {
+  constexpr int N = 6;
+  __shared__ Acc<R> red[(kTailThreads / 32) * N];
+  pdl_trigger();
+  pdl_wait();
+  SolverState* st = b.st + blockIdx.x;
+  if (st->done) return;
+  const int t0 = b.mesh_tile0[blockIdx.x], t1 = b.mesh_tile0[blockIdx.x + 1];
+  Acc<R> s[N] = {};
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) s[k].add(acc_load<R>((const AccStore<R>*)b.part_dir + (size_t)t * N + k));
+  }
+  block_reduce<N, 0xffffffffu, R>(s, red);
+  if (threadIdx.x == 0) {
+    double tot[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) tot[k] = s[k].value();
+    dir_decide<AGB_STABLE_NEO_HOOKEAN>(st, tot);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kGradThreads, 7) batch_grad_kernel(BatchArgs b) {
+  grad_tile<R, AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x],
+                                       (AccStore<R>*)b.part_grad + blockIdx.x);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
+  constexpr int N = 12;
+  constexpr unsigned FF = (1u << 1) | (1u << 6) | (1u << 8) | (1u << 9);
+  __shared__ Acc<R> red[(kVThreads / 32) * N];
+  const SolveArgs& a = b.a;
+  const int c = blockIdx.x;
+  const int v0 = b.chunk_v0[c], v1 = b.chunk_v0[c + 1];
+  const SolverState* st = b.st + b.chunk_mesh[c];
+  pdl_trigger();
+  pdl_wait();
+  if (st->done) return;
+  const R t = (R)st->t;
+  const V4<R>* P = p_cur<R>(a, st->pbuf);
+  R s[N] = {};
+  for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) vertex_update<R>(a, i, a.off[i], a.off[i + 1], t, P, s);
+  Acc<R> acc[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    acc[k] = Acc<R>{};
+    acc[k].add(s[k]);
+  }
+  block_reduce<N, FF, R>(acc, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) ((AccStore<R>*)b.part_vert)[(size_t)c * N + k] = acc_store(acc[k]);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchArgs b) {
+  constexpr int N = 12;
+  __shared__ Acc<R> red[(kTailThreads / 32) * N];
+  __shared__ bool s_last;
+  pdl_wait();
+  SolverState* st = b.st + blockIdx.x;
+  const bool was_done = st->done != 0;  // read by every thread before thread 0 writes it
+  if (!was_done) {
+    const int c0 = b.mesh_chunk0[blockIdx.x], c1 = b.mesh_chunk0[blockIdx.x + 1];
+    Acc<R> s[N] = {};
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) s[k].add(acc_load<R>((const AccStore<R>*)b.part_vert + (size_t)c * N + k));
+    }
+    block_reduce<N, 0xffffffffu, R>(s, red);
+    if (threadIdx.x == 0) {
+      double tot[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k) tot[k] = s[k].value();
+      vertex_decide(st, tot);
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (!st->done) atomicAdd(&b.bs->n_active, 1u);
+    __threadfence();
+    s_last = atomicAdd(&b.bs->arrived, 1u) == (unsigned)b.n_meshes - 1u;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  BatchState* bs = b.bs;
+  const unsigned active = atomicAdd(&bs->n_active, 0u);
+  bs->iter += 1;
+  bs->n_active = 0u;
+  bs->arrived = 0u;
+  if (b.cond)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)b.cond,
+                            (active > 0u && bs->iter < bs->iter_limit) ? 1u : 0u);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kTailThreads) batch_energy_kernel(BatchArgs b) {
+  __shared__ Acc<R> red[kTailThreads / 32];
+  const int t0 = b.mesh_tile0[blockIdx.x], t1 = b.mesh_tile0[blockIdx.x + 1];
+  const double e = block_sum_partials<R>((const AccStore<R>*)b.part_grad + t0, t1 - t0, 1, red);
+  if (threadIdx.x == 0) b.st[blockIdx.x].energy = e + b.st[blockIdx.x].ext_energy;
+}
+
+template <class R>
+__global__ void batch_init_vertex_kernel(BatchArgs b, const R* __restrict__ u, const V4<R>* __restrict__ fixed,
+                                         const int32_t* __restrict__ uoi) {
+  const SolveArgs& a = b.a;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) {
+    const size_t k = 3 * (size_t)uoi[i];
+    const V4<R> fx = fixed[i];
+    const int mask = (int)fx.w;
+    V4<R> x{u[k], u[k + 1], u[k + 2], fx.w};
+    if (mask & 1) x.x = fx.x;
+    if (mask & 2) x.y = fx.y;
+    if (mask & 4) x.z = fx.z;
+    const V4<R> z{R(0), R(0), R(0), R(0)};
+    ((V4<R>*)a.xa)[2 * i] = x;
+    ((V4<R>*)a.xa)[2 * i + 1] = z;
+    ((V4<R>*)a.gd)[2 * i] = z;
+    ((V4<R>*)a.gd)[2 * i + 1] = z;
+    ((V4<R>*)a.p0)[i] = z;
+    ((V4<R>*)a.p1)[i] = z;
+  }
+}
+
+__global__ void batch_init_state_kernel(BatchArgs b, SolverState proto) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < b.n_meshes; m += gridDim.x * blockDim.x) {
+    SolverState st = proto;
+    st.beta = 0.0;
+    st.inv_mean = 1.0;
+    st.gd = st.t = st.alpha0 = st.hq = st.gnorm = st.gnorm0 = st.energy = st.ext_energy = st.delta_e = 0.0;
+    st.iter = 0;
+    st.iter_limit = 0;
+    st.done = 0;
+    st.result = AGB_RUNNING;
+    st.init = 1;
+    st.reset_beta = st.ls_fail = st.ls_steps = st.ls_ok = 0;
+    st.decided = 1;
+    st.error = 0;
+    st.pbuf = 0;
+    b.st[m] = st;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *b.bs = BatchState{0, 0, 0u, 0u};
+}
+
+__global__ void batch_set_limit_kernel(BatchState* bs, int n) { bs->iter_limit = bs->iter + n; }
+
+template <class... P, class... A>
+cudaError_t launch_pdl_b(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+template <class R>
+cudaError_t batch_grad_and_vertex(const BatchArgs& b, cudaStream_t s) {
+  cudaError_t e = launch_pdl_b(batch_grad_kernel<R>, dim3(b.a.fv.n_tiles), dim3(kGradThreads),
+                               grad_smem_bytes<R>(), s, b);
+  if (e == cudaSuccess) e = launch_pdl_b(batch_vertex_kernel<R>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
+  if (e == cudaSuccess)
+    e = launch_pdl_b(batch_vertex_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  return e;
+}
+
+template <class R>
+cudaError_t batch_iteration_t(const BatchArgs& b, cudaStream_t s) {
+  batch_dir_kernel<R><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_pdl_b(batch_dir_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  if (e == cudaSuccess) e = batch_grad_and_vertex<R>(b, s);
+  return e;
+}
+
+template <class R>
+cudaError_t batch_prepare_t() {
+  return cudaFuncSetAttribute(batch_grad_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)grad_smem_bytes<R>());
+}
+
+}  // namespace
+
+cudaError_t batch_prepare_kernels(int precision) {
+  return precision == AGB_F64 ? batch_prepare_t<double>() : batch_prepare_t<float>();
+}
+
+cudaError_t launch_batch_init(const BatchArgs& b, const void* u_user, const void* fixed,
+                              const int32_t* uoi, const SolverState& proto, cudaStream_t s) {
+  const int blocks = b.a.n_points > 0 ? std::min((b.a.n_points + 255) / 256, 4096) : 1;
+  if (b.a.precision == AGB_F64)
+    batch_init_vertex_kernel<double><<<blocks, 256, 0, s>>>(b, (const double*)u_user, (const V4<double>*)fixed, uoi);
+  else
+    batch_init_vertex_kernel<float><<<blocks, 256, 0, s>>>(b, (const float*)u_user, (const V4<float>*)fixed, uoi);
+  batch_init_state_kernel<<<(b.n_meshes + 255) / 256, 256, 0, s>>>(b, proto);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_iteration(const BatchArgs& b, cudaStream_t s) {
+  if (b.a.fv.n_tiles == 0 || b.n_meshes == 0) return cudaErrorInvalidValue;
+  const cudaError_t e =
+      b.a.precision == AGB_F64 ? batch_iteration_t<double>(b, s) : batch_iteration_t<float>(b, s);
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t launch_batch_first(const BatchArgs& b, cudaStream_t s) {
+  if (b.a.fv.n_tiles == 0 || b.n_meshes == 0) return cudaErrorInvalidValue;
+  const cudaError_t e =
+      b.a.precision == AGB_F64 ? batch_grad_and_vertex<double>(b, s) : batch_grad_and_vertex<float>(b, s);
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t launch_batch_set_limit(const BatchArgs& b, int n, cudaStream_t s) {
+  batch_set_limit_kernel<<<1, 1, 0, s>>>(b.bs, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_energy(const BatchArgs& b, cudaStream_t s) {
+  if (b.n_meshes == 0) return cudaSuccess;
+  if (b.a.precision == AGB_F64)
+    batch_energy_kernel<double><<<b.n_meshes, kTailThreads, 0, s>>>(b);
+  else
+    batch_energy_kernel<float><<<b.n_meshes, kTailThreads, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+}  // namespace agb

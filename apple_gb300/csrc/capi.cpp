@@ -976,4 +976,320 @@ int agb_fem_grad_param_vjp(agb_fem* f, const void* u, const void* w, void* out_m
   return AGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// batched PNCG
+// ---------------------------------------------------------------------------
+int agb_batch_destroy(agb_batch* b) {
+  if (!b) return AGB_OK;
+  if (b->loop_exec) cudaGraphExecDestroy(b->loop_exec);
+  if (b->step_exec) cudaGraphExecDestroy(b->step_exec);
+  if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+  for (void* p : {(void*)b->d_tile_estart, (void*)b->d_tile_vstart, (void*)b->d_tile_gstart,
+                  (void*)b->d_group_estart, (void*)b->d_tv_vid, b->d_rec, (void*)b->d_ids,
+                  (void*)b->d_slot_of_tv, (void*)b->d_off, (void*)b->d_uoi, b->d_fixed, b->d_force,
+                  (void*)b->d_tile_mesh, (void*)b->d_mesh_tile0, (void*)b->d_chunk_v0, (void*)b->d_chunk_mesh,
+                  (void*)b->d_mesh_chunk0, b->d_xa, b->d_gd, b->d_p0, b->d_p1, b->d_slots, b->d_part,
+                  (void*)b->d_state, (void*)b->d_bstate})
+    dfree(p);
+  if (b->h_state) cudaFreeHost(b->h_state);
+  delete b;
+  return AGB_OK;
+}
+
+int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_params* params,
+                     int32_t chunk_verts, agb_batch** out) {
+  AGB_REQUIRE(out && n_models > 0 && models, AGB_E_INVALID, "agb_batch_create: bad arguments");
+  *out = nullptr;
+  const int prec = models[0]->precision;
+  for (int k = 0; k < n_models; ++k) {
+    agb_model* m = models[k];
+    AGB_REQUIRE(m && !m->fems.empty(), AGB_E_INVALID, "agb_batch_create: model %d has no FEM potential", k);
+    AGB_REQUIRE(m->precision == prec, AGB_E_INVALID, "agb_batch_create: models must share a precision");
+    for (agb_fem* f : m->fems)
+      AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN, AGB_E_INVALID,
+                  "agb_batch_create: the batched form runs stable Neo-Hookean potentials");
+  }
+  agb_pncg_params prm;
+  agb_pncg_default_params(&prm);
+  if (params) prm = *params;
+  AGB_REQUIRE(prm.max_steps >= 0 && prm.max_backtracking >= 0 && prm.max_backtracking <= 60, AGB_E_INVALID,
+              "agb_batch_create: bad parameters");
+  if (chunk_verts <= 0) chunk_verts = 512;
+  agb_batch* b = new (std::nothrow) agb_batch();
+  AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_create: out of host memory");
+  b->models.assign(models, models + n_models);
+  b->params = prm;
+  b->precision = prec;
+  b->chunk_verts = chunk_verts;
+  // concatenation: vertices, tiles, slots, CSR, DOF data
+  TilePlan& P = b->plan;
+  P.tile_estart.assign(1, 0);
+  P.tile_vstart.assign(1, 0);
+  P.tile_gstart.assign(1, 0);
+  P.group_estart.clear();
+  std::vector<int32_t> slot_of_tv, off(1, 0), uoi, tile_mesh, mesh_tile0(1, 0), chunk_v0(1, 0), chunk_mesh,
+      mesh_chunk0(1, 0);
+  std::vector<double> fixed, force;
+  std::vector<uint8_t> mask;
+  bool any_force = false;
+  b->vert_off.assign(1, 0);
+  for (int k = 0; k < n_models; ++k) {
+    agb_model* m = models[k];
+    const int voff = b->vert_off.back(), np = m->space->n_points;
+    const int soff = off.back();
+    for (size_t q = 0; q < m->fems.size(); ++q) {
+      const TilePlan& Q = m->fems[q]->plan;
+      const int eoff = P.n_cells, tvoff = P.n_tv, goff = (int)P.group_estart.size();
+      for (int t = 0; t < Q.n_tiles; ++t) {
+        P.tile_estart.push_back(eoff + Q.tile_estart[t + 1]);
+        P.tile_vstart.push_back(tvoff + Q.tile_vstart[t + 1]);
+        P.tile_gstart.push_back(goff + Q.tile_gstart[t + 1]);
+        tile_mesh.push_back(k);
+      }
+      for (size_t g = 0; g + 1 < Q.group_estart.size(); ++g) P.group_estart.push_back(eoff + Q.group_estart[g]);
+      for (int32_t v : Q.tv_vid) P.tv_vid.push_back(voff + v);
+      P.ids.insert(P.ids.end(), Q.ids.begin(), Q.ids.end());
+      P.mudv.insert(P.mudv.end(), Q.mudv.begin(), Q.mudv.end());
+      P.lamdv.insert(P.lamdv.end(), Q.lamdv.begin(), Q.lamdv.end());
+      for (int32_t sl : m->slots[q].slot_of_tv) slot_of_tv.push_back(soff + sl);
+      P.n_cells += Q.n_cells;
+      P.n_tv += Q.n_tv;
+      P.n_tiles += Q.n_tiles;
+    }
+    mesh_tile0.push_back(P.n_tiles);
+    for (int i = 0; i < np; ++i) off.push_back(soff + m->off[i + 1]);
+    for (int i = 0; i < np; ++i) uoi.push_back(voff + m->space->user_of_internal[i]);
+    fixed.insert(fixed.end(), m->fixed_internal.begin(), m->fixed_internal.end());
+    mask.insert(mask.end(), m->mask_internal.begin(), m->mask_internal.end());
+    force.insert(force.end(), m->force_internal.begin(), m->force_internal.end());
+    any_force = any_force || m->n_force > 0;
+    for (int v = 0; v < np; v += chunk_verts) {
+      chunk_v0.push_back(voff + std::min(np, v + chunk_verts));
+      chunk_mesh.push_back(k);
+    }
+    mesh_chunk0.push_back((int32_t)chunk_mesh.size());
+    b->vert_off.push_back(voff + np);
+  }
+  P.group_estart.push_back(P.n_cells);
+  P.D.assign(9 * (size_t)P.n_cells, 0.0);
+  {
+    size_t eoff = 0;
+    for (agb_model* m : b->models)
+      for (agb_fem* f : m->fems) {
+        const TilePlan& Q = f->plan;
+        for (int c = 0; c < 9; ++c)
+          std::memcpy(&P.D[(size_t)c * P.n_cells + eoff], &Q.D[(size_t)c * Q.n_cells], sizeof(double) * Q.n_cells);
+        eoff += Q.n_cells;
+      }
+  }
+  b->n_slots = off.back();
+  const int np = b->vert_off.back();
+  const int n_chunks = (int)chunk_mesh.size();
+  const size_t v4 = v4_bytes(prec);
+  int rc = dupload(&b->d_tile_estart, P.tile_estart);
+  if (!rc) rc = dupload(&b->d_tile_vstart, P.tile_vstart);
+  if (!rc) rc = dupload(&b->d_tile_gstart, P.tile_gstart);
+  if (!rc) rc = dupload(&b->d_group_estart, P.group_estart);
+  if (!rc) rc = dupload(&b->d_tv_vid, P.tv_vid);
+  if (!rc) rc = upload_records(P, prec, &b->d_rec, &b->d_ids);
+  if (!rc) rc = dupload(&b->d_slot_of_tv, slot_of_tv);
+  if (!rc) rc = dupload(&b->d_off, off);
+  if (!rc) rc = dupload(&b->d_uoi, uoi);
+  if (!rc) rc = dupload(&b->d_tile_mesh, tile_mesh);
+  if (!rc) rc = dupload(&b->d_mesh_tile0, mesh_tile0);
+  if (!rc) rc = dupload(&b->d_chunk_v0, chunk_v0);
+  if (!rc) rc = dupload(&b->d_chunk_mesh, chunk_mesh);
+  if (!rc) rc = dupload(&b->d_mesh_chunk0, mesh_chunk0);
+  if (!rc) rc = dalloc_bytes(&b->d_fixed, v4 * np);
+  if (!rc) {
+    if (prec == AGB_F64) {
+      auto h = pack_v4<double>(fixed, &mask);
+      rc = upload(b->d_fixed, h.data(), v4 * np);
+    } else {
+      auto h = pack_v4<float>(fixed, &mask);
+      rc = upload(b->d_fixed, h.data(), v4 * np);
+    }
+  }
+  if (!rc && any_force) {
+    rc = dalloc_bytes(&b->d_force, v4 * np);
+    if (!rc) {
+      if (prec == AGB_F64) {
+        auto h = pack_v4<double>(force, nullptr);
+        rc = upload(b->d_force, h.data(), v4 * np);
+      } else {
+        auto h = pack_v4<float>(force, nullptr);
+        rc = upload(b->d_force, h.data(), v4 * np);
+      }
+    }
+  }
+  if (!rc) rc = dalloc_bytes(&b->d_xa, 2 * v4 * np);
+  if (!rc) rc = dalloc_bytes(&b->d_gd, 2 * v4 * np);
+  if (!rc) rc = dalloc_bytes(&b->d_p0, v4 * np);
+  if (!rc) rc = dalloc_bytes(&b->d_p1, v4 * np);
+  if (!rc) rc = dalloc_bytes(&b->d_slots, 2 * v4 * (size_t)b->n_slots);
+  const size_t n_part = (size_t)P.n_tiles * 7 + (size_t)n_chunks * 12;
+  if (!rc) rc = dalloc_bytes(&b->d_part, 8 * n_part);
+  if (!rc) rc = dalloc(&b->d_state, (size_t)n_models);
+  if (!rc) rc = dalloc(&b->d_bstate, 1);
+  if (!rc && cudaMallocHost((void**)&b->h_state, sizeof(SolverState) * n_models) != cudaSuccess) rc = AGB_E_CUDA;
+  if (!rc && cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking) != cudaSuccess) rc = AGB_E_CUDA;
+  if (!rc && batch_prepare_kernels(prec) != cudaSuccess) rc = AGB_E_CUDA;
+  if (rc) {
+    if (rc == AGB_E_CUDA && agb::last_error()[0] == 0) set_error("agb_batch_create: CUDA allocation failed");
+    agb_batch_destroy(b);
+    return rc;
+  }
+  BatchArgs& ba = b->args;
+  SolveArgs& a = ba.a;
+  a.fv.material = AGB_STABLE_NEO_HOOKEAN;
+  a.fv.n_tiles = P.n_tiles;
+  a.fv.n_cells = P.n_cells;
+  a.fv.tile_estart = b->d_tile_estart;
+  a.fv.tile_vstart = b->d_tile_vstart;
+  a.fv.tile_gstart = b->d_tile_gstart;
+  a.fv.group_estart = b->d_group_estart;
+  a.fv.tv_vid = b->d_tv_vid;
+  a.fv.rec = b->d_rec;
+  a.fv.ids = b->d_ids;
+  a.n_points = np;
+  a.precision = prec;
+  a.xa = b->d_xa;
+  a.gd = b->d_gd;
+  a.p0 = b->d_p0;
+  a.p1 = b->d_p1;
+  a.force = b->d_force;
+  a.slot_of_tv = b->d_slot_of_tv;
+  a.off = b->d_off;
+  a.slots = b->d_slots;
+  a.n_slots = b->n_slots;
+  a.st = nullptr;
+  a.max_bt = prm.max_backtracking;
+  ba.n_meshes = n_models;
+  ba.n_chunks = n_chunks;
+  ba.tile_mesh = b->d_tile_mesh;
+  ba.mesh_tile0 = b->d_mesh_tile0;
+  ba.chunk_v0 = b->d_chunk_v0;
+  ba.chunk_mesh = b->d_chunk_mesh;
+  ba.mesh_chunk0 = b->d_mesh_chunk0;
+  ba.st = b->d_state;
+  ba.bs = b->d_bstate;
+  char* part = (char*)b->d_part;
+  ba.part_dir = part;
+  ba.part_grad = part + 8 * (size_t)P.n_tiles * 6;
+  ba.part_vert = part + 8 * (size_t)P.n_tiles * 7;
+  ba.cond = 0;
+  // initial state: done until reset
+  std::vector<SolverState> st0(n_models);
+  for (auto& st : st0) {
+    st = SolverState{};
+    st.done = 1;
+    st.result = AGB_RUNNING;
+  }
+  RC(upload(b->d_state, st0.data(), sizeof(SolverState) * n_models));
+  *out = b;
+  return AGB_OK;
+}
+
+int agb_batch_info(agb_batch* b, int32_t* n_points, int32_t* n_cells) {
+  AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_info: null handle");
+  if (n_points) *n_points = b->vert_off.back();
+  if (n_cells) *n_cells = b->plan.n_cells;
+  return AGB_OK;
+}
+
+int agb_batch_reset(agb_batch* b, const void* u, void* stream) {
+  AGB_REQUIRE(b && u, AGB_E_INVALID, "agb_batch_reset: null argument");
+  cudaStream_t s = as_stream(stream);
+  SolverState proto{};
+  proto.rtol = b->params.rtol;
+  proto.atol = b->params.atol;
+  proto.armijo_c = b->params.armijo_c;
+  proto.overstep = b->params.overstep;
+  proto.beta_max = b->params.beta_max;
+  proto.max_steps = b->params.max_steps;
+  proto.max_bt = b->params.max_backtracking;
+  RC(check_launch(launch_batch_init(b->args, u, b->d_fixed, b->d_uoi, proto, s), "batch_init"));
+  RC(check_launch(launch_batch_first(b->args, s), "batch_first"));
+  return AGB_OK;
+}
+
+static int build_batch_graph(agb_batch* b, bool loop) {
+  cudaGraph_t g = nullptr;
+  AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
+  cudaGraph_t body = g;
+  cudaGraphConditionalHandle h = 0;
+  cudaError_t e = cudaSuccess;
+  if (loop) {
+    e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (e == cudaSuccess) body = np.conditional.phGraph_out[0];
+  }
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(b->capture_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    BatchArgs a = b->args;
+    a.cond = loop ? (unsigned long long)h : 0ull;
+    cudaError_t le = launch_batch_iteration(a, b->capture_stream);
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(b->capture_stream, &captured);
+    if (e == cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(loop ? &b->loop_exec : &b->step_exec, g, 0);
+  cudaGraphDestroy(g);
+  return check_launch(e, loop ? "batch loop graph" : "batch step graph");
+}
+
+int agb_batch_iterate(agb_batch* b, int32_t n_steps, void* stream) {
+  AGB_REQUIRE(b && n_steps >= 0, AGB_E_INVALID, "agb_batch_iterate: bad argument");
+  if (n_steps == 0) return AGB_OK;
+  if (!b->loop_exec) RC(build_batch_graph(b, true));
+  cudaStream_t s = as_stream(stream);
+  RC(check_launch(launch_batch_set_limit(b->args, n_steps, s), "batch_set_limit"));
+  AGB_CHECK_CUDA(cudaGraphLaunch(b->loop_exec, s));
+  return AGB_OK;
+}
+
+int agb_batch_step(agb_batch* b, void* stream) {
+  AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_step: null handle");
+  if (!b->step_exec) RC(build_batch_graph(b, false));
+  AGB_CHECK_CUDA(cudaGraphLaunch(b->step_exec, as_stream(stream)));
+  return AGB_OK;
+}
+
+int agb_batch_read(agb_batch* b, void* u_out, agb_pncg_stats* stats, void* stream) {
+  AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_read: null handle");
+  cudaStream_t s = as_stream(stream);
+  if (u_out) {
+    SolveArgs a = b->args.a;
+    RC(check_launch(launch_solver_unpack_x(a, nullptr, b->d_uoi, u_out, s), "batch unpack"));
+  }
+  RC(check_launch(launch_batch_energy(b->args, s), "batch_energy"));
+  const int n = (int)b->models.size();
+  AGB_CHECK_CUDA(cudaMemcpyAsync(b->h_state, b->d_state, sizeof(SolverState) * n, cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    for (int k = 0; k < n; ++k) {
+      const SolverState& st = b->h_state[k];
+      stats[k].result = st.done ? st.result : AGB_RUNNING;
+      stats[k].n_steps = st.iter;
+      stats[k].grad_norm = st.gnorm;
+      stats[k].grad_norm_first = st.gnorm0;
+      stats[k].energy = st.energy;
+      stats[k].alpha = st.ls_ok ? st.t : 0.0;
+      stats[k].beta = st.beta;
+      stats[k].line_search_steps = st.ls_steps;
+      stats[k].line_search_ok = st.ls_ok;
+    }
+  }
+  for (int k = 0; k < n; ++k)
+    AGB_REQUIRE(b->h_state[k].error == 0, AGB_E_DEVICE, "batch: device guard tripped in model %d", k);
+  return AGB_OK;
+}
+
 }  // extern "C"

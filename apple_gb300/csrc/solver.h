@@ -127,6 +127,43 @@ struct CgArgs {
   unsigned long long cond;
 };
 
+// Batched PNCG (batch.cu): independent meshes concatenated into one vertex
+// and tile set; every mesh has its own SolverState and its own reductions.
+struct BatchState {
+  int32_t iter;        // iterations of the batch loop
+  int32_t iter_limit;
+  uint32_t n_active;   // meshes still running after this iteration (vertex tail)
+  uint32_t arrived;    // vertex-tail CTAs finished (last one sets the condition)
+};
+
+struct BatchArgs {
+  SolveArgs a;                 // concatenated meshes (a.st unused)
+  int n_meshes;
+  int n_chunks;
+  const int32_t* tile_mesh;    // n_tiles
+  const int32_t* mesh_tile0;   // n_meshes + 1
+  const int32_t* chunk_v0;     // n_chunks + 1 vertex ranges, each inside one mesh
+  const int32_t* chunk_mesh;   // n_chunks
+  const int32_t* mesh_chunk0;  // n_meshes + 1
+  SolverState* st;             // n_meshes
+  BatchState* bs;
+  void* part_dir;              // n_tiles x 6
+  void* part_grad;             // n_tiles
+  void* part_vert;             // n_chunks x 12
+  unsigned long long cond;
+};
+
+cudaError_t batch_prepare_kernels(int precision);
+cudaError_t launch_batch_init(const BatchArgs& b, const void* u_user, const void* fixed,
+                              const int32_t* user_of_internal, const SolverState& proto, cudaStream_t s);
+// one iteration of every running mesh: direction pass + tail, gradient pass,
+// vertex pass + tail
+cudaError_t launch_batch_iteration(const BatchArgs& b, cudaStream_t s);
+// gradient + vertex pass at t = 0 (g_0, diag_0 of every mesh)
+cudaError_t launch_batch_first(const BatchArgs& b, cudaStream_t s);
+cudaError_t launch_batch_set_limit(const BatchArgs& b, int n, cudaStream_t s);
+cudaError_t launch_batch_energy(const BatchArgs& b, cudaStream_t s);
+
 cudaError_t cg_prepare_kernels(int precision);
 size_t cg_smem(int precision);
 cudaError_t launch_cg_init(const CgArgs& c, const void* rhs_user, const int32_t* user_of_internal,
@@ -179,6 +216,47 @@ struct agb_solver {
   agb::CgArgs cg{};
   cudaGraphExec_t cg_exec = nullptr;
   // graphs
+  cudaGraphExec_t loop_exec = nullptr;
+  cudaGraphExec_t step_exec = nullptr;
+  cudaStream_t capture_stream = nullptr;
+};
+
+struct agb_batch {
+  std::vector<agb_model*> models;
+  agb_pncg_params params{};
+  int precision = 0;
+  int chunk_verts = 0;
+  std::vector<int32_t> vert_off;  // per model, n_models + 1 (concatenated vertex ids)
+  agb::TilePlan plan;             // concatenated tiles (tv_vid in concatenated ids)
+  int32_t n_slots = 0;
+  // device
+  int32_t* d_tile_estart = nullptr;
+  int32_t* d_tile_vstart = nullptr;
+  int32_t* d_tile_gstart = nullptr;
+  int32_t* d_group_estart = nullptr;
+  int32_t* d_tv_vid = nullptr;
+  void* d_rec = nullptr;
+  uint32_t* d_ids = nullptr;
+  int32_t* d_slot_of_tv = nullptr;
+  int32_t* d_off = nullptr;
+  int32_t* d_uoi = nullptr;        // concatenated user_of_internal
+  void* d_fixed = nullptr;         // V4<R>, w = mask bits
+  void* d_force = nullptr;         // V4<R> or null
+  int32_t* d_tile_mesh = nullptr;
+  int32_t* d_mesh_tile0 = nullptr;
+  int32_t* d_chunk_v0 = nullptr;
+  int32_t* d_chunk_mesh = nullptr;
+  int32_t* d_mesh_chunk0 = nullptr;
+  void* d_xa = nullptr;
+  void* d_gd = nullptr;
+  void* d_p0 = nullptr;
+  void* d_p1 = nullptr;
+  void* d_slots = nullptr;
+  void* d_part = nullptr;
+  agb::SolverState* d_state = nullptr;
+  agb::SolverState* h_state = nullptr;  // pinned, n_meshes
+  agb::BatchState* d_bstate = nullptr;
+  agb::BatchArgs args{};
   cudaGraphExec_t loop_exec = nullptr;
   cudaGraphExec_t step_exec = nullptr;
   cudaStream_t capture_stream = nullptr;

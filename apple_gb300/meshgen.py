@@ -152,3 +152,26 @@ def lumped_gravity(mesh: TetMesh, rho: float, g=(0.0, 0.0, -9.8)) -> np.ndarray:
     m = np.zeros(mesh.n_points)
     np.add.at(m, mesh.cells.ravel(), np.repeat(vol / 4.0, 4))
     return rho * m[:, None] * np.asarray(g, np.float64)[None, :]
+
+
+def batch_case(k: int, rng: np.random.Generator, dims=(4, 40), h: float = 0.05):
+    """One mesh of the batched workload: a grid with (nx, ny, nz) ~ U{dims}
+    cells per axis, stable Neo-Hookean with E ~ U[1e3, 1e5], nu ~ U[0.3, 0.49],
+    density 1000, one random Dirichlet face (all three components fixed) and
+    a random gravity direction.  Returns (mesh with FixedMask / FixedValue and
+    mu / lambda cell data, per-vertex force)."""
+    nx, ny, nz = (int(v) for v in rng.integers(dims[0], dims[1] + 1, size=3))
+    m = grid(nx, ny, nz, h=h)
+    E = float(rng.uniform(1e3, 1e5))
+    nu = float(rng.uniform(0.3, 0.49))
+    lam, mu = lame_converter(E, nu)
+    m.cell_data["mu"] = np.full(m.n_cells, mu)
+    m.cell_data["lambda"] = np.full(m.n_cells, lam)
+    face = int(rng.integers(0, 6))
+    mask = np.zeros((m.n_points, 3), bool)
+    mask[face_mask(m, face // 2, "min" if face % 2 == 0 else "max")] = True
+    m.point_data["FixedMask"] = mask
+    m.point_data["FixedValue"] = np.zeros((m.n_points, 3))
+    g = rng.normal(size=3)
+    g *= 9.8 / np.linalg.norm(g)
+    return m, lumped_gravity(m, 1000.0, g)

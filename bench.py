@@ -55,6 +55,11 @@ def _args():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
+    ap.add_argument("--config", choices=["plain", "adjoint", "batched"], default="plain",
+                    help="plain: the headline PNCG line; adjoint: the 138k-tet adjoint workload; "
+                         "batched: 512 uneven meshes in one batch vs solved one by one")
+    ap.add_argument("--n-meshes", type=int, default=512, help="batched: number of meshes")
+    ap.add_argument("--fd-cells", type=int, default=32, help="adjoint: cells checked by central differences")
     ap.add_argument("--profile", action="store_true",
                     help="run warmup iterations, then each pass `steps` times as plain launches (ncu captures)")
     return ap.parse_args()
@@ -341,10 +346,226 @@ def run_ours(a) -> None:
         dist.destroy_process_group()
 
 
+ADJ_WORKLOAD = "snh_grid_24x24x48_138k_tets_stretch30_theta_mu"
+
+
+def run_adjoint(a) -> None:
+    """The adjoint workload: dL/dtheta for per-tet theta scaling mu, by the
+    device adjoint (forward PNCG to 1e-7 in FP32, CG, material VJP), checked
+    against central differences of the FP64 forward on `fd_cells` cells."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+    from apple_gb300.adjoint import MaterialEquilibrium
+
+    rng = np.random.default_rng(0)
+    nx, ny, nz = (6, 6, 12) if a.small else (24, 24, 48)
+    m = meshgen.grid(nx, ny, nz, h=1.0 / nx)
+    lam0, mu0 = meshgen.lame_converter(E_MOD, NU)
+    theta = rng.uniform(0.5, 2.0, m.n_cells)
+    theta_star = rng.uniform(0.5, 2.0, m.n_cells)
+    mask = np.zeros((m.n_points, 3), bool)
+    fv = np.zeros((m.n_points, 3))
+    mask[meshgen.face_mask(m, 2, "min")] = True
+    top = meshgen.face_mask(m, 2, "max")
+    mask[top] = True
+    fv[top, 2] = STRETCH * m.points[:, 2].max()
+    surf = np.zeros(m.n_points, bool)
+    for ax in range(3):
+        for side in ("min", "max"):
+            surf |= meshgen.face_mask(m, ax, side)
+    mesh = meshgen.TetMesh(m.points, m.cells)
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = fv
+    lam = lam0 * np.ones(m.n_cells)
+    crit32 = ag.ConvergenceCriteria(max_steps=200000, rtol=1e-7)
+    crit64 = ag.ConvergenceCriteria(max_steps=200000, rtol=1e-10)
+    p32 = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float32, criteria=crit32, cg_rtol=1e-6)
+    p64 = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float64, criteria=crit64, cg_rtol=1e-10)
+    dev = torch.device("cuda")
+    si = torch.tensor(np.flatnonzero(surf), device=dev)
+
+    target = p64.solve(mu0 * theta_star, lam)[si].clone()
+
+    def loss(u):
+        return 0.5 * float(((u.double()[si] - target) ** 2).sum())
+
+    def gradient(prob, th):
+        u = prob.solve(mu0 * th, lam)
+        g = torch.zeros_like(u)
+        g[si] = (u.double()[si] - target).to(u.dtype)
+        d = prob.vjp(g)["mu"].double().cpu().numpy() * mu0  # dL/dtheta = dL/dmu * mu0
+        return loss(u), d, dict(prob.timings), prob.stats
+
+    gradient(p32, theta)  # warm-up (graph capture, kernel attributes)
+    L32, d32, t32, s32 = gradient(p32, theta)
+    L64, d64, t64, s64 = gradient(p64, theta)
+    cells = rng.choice(m.n_cells, size=min(a.fd_cells, m.n_cells), replace=False)
+    fd = []
+    t_fd0 = time.perf_counter()
+    for c in cells:
+        h = 1e-4 * theta[c]
+        vals = []
+        for sgn in (1.0, -1.0):
+            th = theta.copy()
+            th[c] += sgn * h
+            vals.append(loss(p64.solve(mu0 * th, lam)))
+        fd.append((vals[0] - vals[1]) / (2 * h))
+    t_fd = time.perf_counter() - t_fd0
+    fd = np.asarray(fd)
+
+    def rel(x, y):
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+
+    fwd32 = t32["forward"]
+    adj32 = t32["adjoint"]
+    line = {
+        "metric": "adjoint dL/dtheta: s per full gradient (forward + adjoint) vs central differences",
+        "config": {"workload": ADJ_WORKLOAD if not a.small else "snh_grid_6x6x12_adjoint", "n_tets": m.n_cells,
+                   "n_vertices": m.n_points, "n_params": m.n_cells, "E": E_MOD, "nu": NU,
+                   "loss": "0.5 ||u_surface - u_target||^2, u_target from hidden theta*",
+                   "forward_rtol_f32": 1e-7, "cg_rtol_f32": 1e-6, "fd_step": "1e-4 theta (FP64 forward)"},
+        "f32": {"forward_s": fwd32, "forward_iters": s32.forward.n_steps, "adjoint_s": adj32,
+                "cg_iters": s32.cg.n_iter, "gradient_s": fwd32 + adj32,
+                "rel_err_vs_fd": rel(d32[cells], fd), "rel_err_vs_f64_adjoint": rel(d32, d64)},
+        "f64": {"forward_s": t64["forward"], "forward_iters": s64.forward.n_steps, "adjoint_s": t64["adjoint"],
+                "cg_iters": s64.cg.n_iter, "rel_err_vs_fd": rel(d64[cells], fd)},
+        "fd": {"cells": int(len(cells)), "seconds": t_fd, "seconds_per_param": t_fd / max(len(cells), 1)},
+        "adjoint_vs_plain": {
+            "plain": "central differences of the plain forward, 2 solves per parameter",
+            "plain_s_all_params_f32_est": 2 * m.n_cells * fwd32,
+            "adjoint_s_f32": fwd32 + adj32,
+            "speedup_est": 2 * m.n_cells * fwd32 / (fwd32 + adj32),
+            "adjoint_over_forward": adj32 / fwd32,
+        },
+        "dtype": "f32 (and f64 check)", "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
+BATCH_WORKLOAD = "snh_batch_512_grids_4to40_cells_per_axis"
+
+
+def _batch_models(cases, dtype, tile_elems=0, workers=16):
+    """Models of the batched workload, built on host threads (the C ABI set-up
+    releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+
+    def build(case):
+        m, f = case
+        pot = ag.StableNeoHookean.from_pyvista(m, dtype=dtype, tile_elems=tile_elems)
+        b = ag.ModelBuilder(dtype=dtype)
+        b.add_vertices(m)
+        b.add_fixed(m)
+        b.add_potential(pot)
+        fm = meshgen.TetMesh(m.points, m.cells)
+        fm.point_data["Force"] = f
+        fm.point_data["GlobalPointId"] = np.arange(m.n_points)
+        b.add_potential(ag.ExternalForce.from_pyvista(fm, dtype=dtype))
+        model = b.finalize()
+        model.warp_model.handle  # create the device model on this thread
+        return model
+
+    import numpy as np
+
+    with ThreadPoolExecutor(workers) as ex:
+        return list(ex.map(build, cases))
+
+
+def run_batched(a) -> None:
+    """The batched workload: all meshes in one batch (one graph launch per
+    iteration of every running mesh) vs the plain per-mesh solve."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+    from apple_gb300.batch import BatchedForward, autotune
+    from oracle import fem_oracle as O
+
+    n = 24 if a.small else a.n_meshes
+    dims = (4, 12) if a.small else (4, 40)
+    rng = np.random.default_rng(0)
+    cases = [meshgen.batch_case(k, rng, dims=dims, h=1.0 / 40) for k in range(n)]
+    crit = ag.ConvergenceCriteria(max_steps=50000, rtol=1e-6)
+    dtype = torch.float32
+    t0 = time.perf_counter()
+    sub = [cases[i] for i in np.random.default_rng(1).choice(n, size=min(24, n), replace=False)]
+    tune = autotune(lambda te: _batch_models(sub, dtype, te), iters=5, optimizer=ag.PNCG(crit))
+    t_tune = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    models = _batch_models(cases, dtype, tune.tile_elems)
+    t_build = time.perf_counter() - t0
+    bf = BatchedForward(models, ag.PNCG(crit), chunk_verts=tune.chunk_verts)
+    n_points, n_cells = bf.info()
+    bf.solve(max_steps=3)  # warm-up: graph capture
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bf.reset()
+    bf.iterate(crit.max_steps)
+    sols, us = bf.read()
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    # plain: every model on its own (reset + iterate graph + read), in sequence
+    plain_u, plain_sols, t_plain = [], [], 0.0
+    for mdl in models:
+        opt = ag.PNCG(crit)
+        fwd = ag.Forward(mdl, opt)
+        opt.solver(fwd.problem)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        sol = fwd.step()
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t1
+        plain_sols.append(sol)
+        plain_u.append(fwd.state.u)
+    diag = [float(np.linalg.norm(m.points.max(0) - m.points.min(0))) for m, _ in cases]
+    err_bp = max(float((u.double() - v.double()).abs().max()) / d for u, v, d in zip(us, plain_u, diag))
+    # FP64 oracle on the smallest meshes
+    small = sorted(range(n), key=lambda k: cases[k][0].n_cells)[:4]
+    err_o = []
+    for k in small:
+        m, f = cases[k]
+        ora = O.FemPotential.from_mesh(O.Material.STABLE_NEO_HOOKEAN, m.points, m.cells, mu=m.cell_data["mu"],
+                                       lam=m.cell_data["lambda"])
+        om = O.Model(O.DofMap(m.n_points, m.point_data["FixedMask"], np.zeros((m.n_points, 3))), [ora],
+                     O.ExternalForce(np.arange(m.n_points), f))
+        u_ref, _ = O.solve_model(om, rtol=1e-10, max_steps=50000)
+        err_o.append(float(np.abs(us[k].double().cpu().numpy() - u_ref).max()) / diag[k])
+    iters = np.array([s.n_steps for s in sols])
+    ok = sum(s.result == ag.Result.PRIMARY_SUCCESS for s in sols)
+    ok_plain = sum(s.result == ag.Result.PRIMARY_SUCCESS for s in plain_sols)
+    tet_iters = sum(m.n_cells * s.n_steps for (m, _), s in zip(cases, sols))
+    line = {
+        "metric": "batched vs plain: seconds to solve every mesh to ||g||/||g0|| <= 1e-6",
+        "config": {"workload": BATCH_WORKLOAD if not a.small else "snh_batch_24_grids_4to12", "n_meshes": n,
+                   "n_tets": n_cells, "n_vertices": n_points, "dims_per_axis": list(dims),
+                   "tile_elems": tune.tile_elems, "chunk_verts": tune.chunk_verts},
+        "batched_s": t_batch, "plain_s": t_plain, "speedup": t_plain / t_batch,
+        "batched_tet_iters_per_s": tet_iters / t_batch,
+        "iters": {"mean": float(iters.mean()), "max": int(iters.max()), "min": int(iters.min())},
+        "converged": {"batched": int(ok), "plain": int(ok_plain), "of": n},
+        "max_diff_batched_vs_plain_over_diag": err_bp,
+        "max_err_vs_fp64_oracle_over_diag": max(err_o) if err_o else None,
+        "autotune": {"seconds": t_tune, "table_ms_per_iter": tune.table}, "build_s": t_build,
+        "dtype": "f32", "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == "adjoint":
+        run_adjoint(a)
+    elif a.config == "batched":
+        run_batched(a)
     else:
         run_ours(a)
 

@@ -57,6 +57,7 @@ typedef struct agb_space agb_space;
 typedef struct agb_fem agb_fem;
 typedef struct agb_model agb_model;
 typedef struct agb_solver agb_solver;
+typedef struct agb_batch agb_batch;
 
 const char* agb_last_error(void);
 const char* agb_version(void);
@@ -206,6 +207,30 @@ int agb_solver_time_passes(agb_solver* solver, int32_t reps, void* flush, size_t
 /* Optimizer.minimize(problem, state, free) with HOST buffers: copies u_host
  * in, solves to termination, copies the result back into u_host. */
 int agb_pncg_minimize_host(agb_solver* solver, void* u_host, agb_pncg_stats* stats, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Batched PNCG: independent models (each its own space, stable Neo-Hookean
+ * potentials of one precision, fixed DOFs, external force) solved together.
+ * Every model runs the PNCG iteration above with its own beta, step and
+ * termination; an iteration of all running models is one set of launches
+ * (one CUDA graph).  No reference counterpart: the reference steps one
+ * Forward (forward/_forward.py:52-56) per model.  Vectors are the models'
+ * caller-order displacements concatenated (n_points_total x 3, device);
+ * chunk_verts (0: 512) is the vertex-pass block size.
+ * ------------------------------------------------------------------------- */
+int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_params* params,
+                     int32_t chunk_verts, agb_batch** out);
+int agb_batch_destroy(agb_batch* batch);
+/* totals: concatenated vertices and tets */
+int agb_batch_info(agb_batch* batch, int32_t* n_points, int32_t* n_cells);
+int agb_batch_reset(agb_batch* batch, const void* u, void* stream);
+/* up to n_steps iterations of every running model (one graph launch) */
+int agb_batch_iterate(agb_batch* batch, int32_t n_steps, void* stream);
+/* exactly one iteration as a plain graph */
+int agb_batch_step(agb_batch* batch, void* stream);
+/* u out (device, concatenated caller order; may be NULL) and stats[n_models]
+ * (host); synchronises stream */
+int agb_batch_read(agb_batch* batch, void* u_out, agb_pncg_stats* stats, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Differentiation of the converged equilibrium g(u*, theta) = 0 (the inverse
