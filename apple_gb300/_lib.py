@@ -29,6 +29,7 @@ class PncgParams(ctypes.Structure):
         ("armijo_c", c_double),
         ("overstep", c_double),
         ("beta_max", c_double),
+        ("refresh_ratio", c_double),
     ]
 
 

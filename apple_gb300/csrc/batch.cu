@@ -97,8 +97,7 @@ __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs 
 
 template <class R>
 __global__ void __launch_bounds__(kGradThreads, 7) batch_grad_kernel(BatchArgs b) {
-  grad_tile<R, AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x],
-                                       (AccStore<R>*)b.part_grad + blockIdx.x);
+  grad_tile<R, AGB_STABLE_NEO_HOOKEAN, false>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
 }
 
 template <class R>
@@ -116,7 +115,7 @@ __global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
   const R t = (R)st->t;
   const V4<R>* P = p_cur<R>(a, st->pbuf);
   R s[N] = {};
-  for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) vertex_update<R>(a, i, a.off[i], a.off[i + 1], t, P, s);
+  for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) vertex_update<R, false>(a, i, a.off[i], a.off[i + 1], t, P, s);
   Acc<R> acc[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) {
@@ -169,6 +168,11 @@ __global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchAr
   if (b.cond)
     cudaGraphSetConditional((cudaGraphConditionalHandle)b.cond,
                             (active > 0u && bs->iter < bs->iter_limit) ? 1u : 0u);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kElemThreads) batch_energy_pass_kernel(BatchArgs b) {
+  energy_tile<R, AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x, (AccStore<R>*)b.part_grad + blockIdx.x);
 }
 
 template <class R>
@@ -301,10 +305,13 @@ cudaError_t launch_batch_set_limit(const BatchArgs& b, int n, cudaStream_t s) {
 
 cudaError_t launch_batch_energy(const BatchArgs& b, cudaStream_t s) {
   if (b.n_meshes == 0) return cudaSuccess;
-  if (b.a.precision == AGB_F64)
+  if (b.a.precision == AGB_F64) {
+    batch_energy_pass_kernel<double><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     batch_energy_kernel<double><<<b.n_meshes, kTailThreads, 0, s>>>(b);
-  else
+  } else {
+    batch_energy_pass_kernel<float><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     batch_energy_kernel<float><<<b.n_meshes, kTailThreads, 0, s>>>(b);
+  }
   return cudaGetLastError();
 }
 

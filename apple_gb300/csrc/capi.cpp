@@ -520,6 +520,7 @@ void agb_pncg_default_params(agb_pncg_params* p) {
   p->armijo_c = 1e-4;
   p->overstep = 1.0;
   p->beta_max = 10.0;
+  p->refresh_ratio = -1.0;
 }
 
 int agb_solver_destroy(agb_solver* sv) {
@@ -533,7 +534,7 @@ int agb_solver_destroy(agb_solver* sv) {
   for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tile_gstart,
                   (void*)sv->d_group_estart, (void*)sv->d_tv_vid,
                   (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_xa, sv->d_gd, sv->d_p0,
-                  sv->d_p1, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
+                  sv->d_p1, sv->d_xref, sv->d_gref, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
                   sv->d_u_tmp})
     dfree(p);
   if (sv->h_state) cudaFreeHost(sv->h_state);
@@ -552,8 +553,10 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   agb_pncg_params prm;
   agb_pncg_default_params(&prm);
   if (params) prm = *params;
-  AGB_REQUIRE(prm.max_steps >= 0 && prm.max_backtracking >= 0 && prm.max_backtracking <= 60,
+  AGB_REQUIRE(prm.max_steps >= 0 && prm.max_backtracking >= 0 && prm.max_backtracking <= 60 &&
+                  prm.refresh_ratio < 1.0,
               AGB_E_INVALID, "agb_solver_create: bad parameters");
+  if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-2 : 0.0;
   agb_solver* sv = new (std::nothrow) agb_solver();
   AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_create: out of host memory");
   sv->model = m;
@@ -630,6 +633,9 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   if (!rc) rc = dalloc_bytes(&sv->d_gd, 2 * v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_p0, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_p1, v4 * np);
+  const bool delta = sv->precision == AGB_F32 && mat == AGB_STABLE_NEO_HOOKEAN && prm.refresh_ratio > 0.0;
+  if (!rc && delta) rc = dalloc_bytes(&sv->d_xref, v4 * np);
+  if (!rc && delta) rc = dalloc_bytes(&sv->d_gref, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_slots, v4 * 2 * (size_t)m->n_slots);
   if (!rc) rc = dalloc_bytes(&sv->d_part, 8 * n_part);
   if (!rc) rc = dalloc(&sv->d_cnt, n_cnt);
@@ -652,6 +658,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
     st.done = 1;
     st.result = AGB_RUNNING;
     st.decided = 1;
+    st.ref_ratio = delta ? prm.refresh_ratio : 0.0;
     rc = upload(sv->d_state, &st, sizeof(st));
   }
   if (rc) {
@@ -667,6 +674,9 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.gd = sv->d_gd;
   a.p0 = sv->d_p0;
   a.p1 = sv->d_p1;
+  a.xref = sv->d_xref;
+  a.gref = sv->d_gref;
+  a.delta = delta ? 1 : 0;
   a.force = m->d_force;
   a.slot_of_tv = sv->d_slot_of_tv;
   a.off = m->d_off;
@@ -697,8 +707,29 @@ int agb_solver_reset(agb_solver* sv, const void* u, void* stream) {
   RC(check_launch(launch_solver_init(sv->args, u, sv->model->d_fixed,
                                      sv->model->space->d_user_of_internal, s),
                   "solver_init"));
+  if (sv->args.delta) {  // x_ref = x_0 and g(x_0) in FP64 before the first gradient pass
+    RC(check_launch(launch_solver_force_refresh(sv->args, s), "solver_refresh"));
+    RC(check_launch(launch_solver_refresh(sv->args, s), "solver_refresh"));
+  }
   RC(check_launch(launch_solver_first(sv->args, s), "solver_first"));
   return AGB_OK;
+}
+
+// Capture one solver iteration into `graph` (which is being built: the
+// while body, or a top-level graph).  With the reference-state correction the
+// two refresh passes follow the vertex pass; they return at once unless the
+// vertex pass asked for a refresh.
+static cudaError_t capture_iteration(agb_solver* sv, cudaGraph_t graph, unsigned long long cond) {
+  cudaStream_t cs = sv->capture_stream;
+  SolveArgs a = sv->args;
+  a.cond = cond;
+  cudaError_t e = cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = launch_solver_iteration(a, cond != 0, cs);
+  if (le == cudaSuccess && a.delta) le = launch_solver_refresh(a, cs);
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(cs, &captured);
+  return e == cudaSuccess ? le : e;
 }
 
 static int build_loop_graph(agb_solver* sv) {
@@ -721,17 +752,7 @@ static int build_loop_graph(agb_solver* sv) {
     cudaGraphDestroy(g);
     return check_launch(e, "cudaGraphAddNode(conditional)");
   }
-  cudaGraph_t body = np.conditional.phGraph_out[0];
-  e = cudaStreamBeginCaptureToGraph(sv->capture_stream, body, nullptr, nullptr, 0,
-                                    cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess) {
-    SolveArgs a = sv->args;
-    a.cond = (unsigned long long)h;
-    cudaError_t le = launch_solver_iteration(a, true, sv->capture_stream);
-    cudaGraph_t captured = nullptr;
-    e = cudaStreamEndCapture(sv->capture_stream, &captured);
-    if (e == cudaSuccess) e = le;
-  }
+  e = capture_iteration(sv, np.conditional.phGraph_out[0], (unsigned long long)h);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->loop_exec, g, 0);
   cudaGraphDestroy(g);
   return check_launch(e, "solver loop graph");
@@ -739,12 +760,10 @@ static int build_loop_graph(agb_solver* sv) {
 
 static int build_step_graph(agb_solver* sv) {
   cudaGraph_t g = nullptr;
-  AGB_CHECK_CUDA(cudaStreamBeginCapture(sv->capture_stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t le = launch_solver_iteration(sv->args, false, sv->capture_stream);
-  cudaError_t e = cudaStreamEndCapture(sv->capture_stream, &g);
-  if (e == cudaSuccess) e = le;
+  AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
+  cudaError_t e = capture_iteration(sv, g, 0ull);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->step_exec, g, 0);
-  if (g) cudaGraphDestroy(g);
+  cudaGraphDestroy(g);
   return check_launch(e, "solver step graph");
 }
 

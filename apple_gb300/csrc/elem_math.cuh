@@ -218,6 +218,57 @@ __device__ __forceinline__ void snh_poly(const SnhPoint<R>& s, const SnhDir<R>& 
   c[4] = R(0.5) * lam * d.a3 * d.a3;
 }
 
+// Mixed cofactor: cof(X + D) = cof(X) + mixed_cof(X, D) + cof(D); column c is
+// x_{c+1} x d_{c+2} + d_{c+1} x x_{c+2} (columns of X and D, indices mod 3).
+template <class R>
+__device__ __forceinline__ void mixed_cof(const R (&X)[3][3], const R (&D)[3][3], R (&B)[3][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+      B[i][c] = X[i1][c1] * D[i2][c2] - X[i2][c1] * D[i1][c2] + D[i1][c1] * X[i2][c2] - D[i2][c1] * X[i1][c2];
+    }
+  }
+}
+
+// P(A + D) - P(A) for stable Neo-Hookean, expanded exactly so that no O(1)
+// term cancels: with F = I + A,
+//   cof(A+D) - cof(A) = B(A,D) + cof(D),   cof(F+D) - cof(F) = tr(D) I - D^T + B(A,D) + cof(D),
+//   J(F+D) - J(F) = cof F : D + F : cof D + det D,
+//   dP = mu (D + D^T - tr(D) I - dcof(A)) + lambda ((J-1) dcof(F) + dJ cof(F+D)).
+// Every term is a product with D, so FP32 keeps relative accuracy in dP.
+// `s` is the state at A; `s2` receives the state at A + D (G, cof F, J - 1;
+// rounded, for the diagonal and the energy).
+template <class R>
+__device__ __forceinline__ void snh_pk1_delta(const SnhPoint<R>& s, const R (&D)[3][3], R mu, R lam,
+                                              R (&dP)[3][3], SnhPoint<R>& s2) {
+  R cD[3][3], dcA[3][3];
+  cof3(D, cD);
+  mixed_cof(s.G, D, dcA);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dcA[i][j] += cD[i][j];
+  const R trD = D[0][0] + D[1][1] + D[2][2];
+  const R a1 = ddot3(s.cofF, D);
+  const R a2 = (cD[0][0] + cD[1][1] + cD[2][2]) + ddot3(s.G, cD);
+  const R dJ = a1 + a2 + det3(D);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const R dcF = (i == j ? trD : R(0)) - D[j][i] + dcA[i][j];
+      const R cF2 = s.cofF[i][j] + dcF;
+      const R dfc = D[i][j] + D[j][i] - (i == j ? trD : R(0)) - dcA[i][j];
+      dP[i][j] = mu * dfc + lam * (s.jm1 * dcF + dJ * cF2);
+      s2.G[i][j] = s.G[i][j] + D[i][j];
+      s2.cofF[i][j] = cF2;
+    }
+  s2.jm1 = s.jm1 + dJ;
+}
+
 // H_e p as a 3x3 M with corner forces M D_a^T (h3_prod, h5_prod, h6_prod)
 template <class R>
 __device__ __forceinline__ void snh_hess_prod(const SnhPoint<R>& s, const SnhDir<R>& d,

@@ -61,8 +61,10 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   __shared__ Acc<R> red[kWarps * N];
   SolverState* st = a.st;
   pdl_trigger();
-  if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
-    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
+    st->refresh = 0;  // the refresh passes, if any, ran after the last vertex pass
+  }
   static_assert(kTileVerts == kElemThreads, "one staged vertex per thread");
   int tile = blockIdx.x;
   // constant inputs first: the thread's first element record and vertex id
@@ -222,15 +224,15 @@ size_t solver_grad_smem(int precision) {
   return precision == AGB_F64 ? grad_smem_bytes<double>() : grad_smem_bytes<float>();
 }
 
-template <class R, int MAT>
+template <class R, int MAT, bool DELTA>
 __global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 7 : 5) solver_grad_kernel(SolveArgs a) {
-  grad_tile<R, MAT>(a, blockIdx.x, a.st, (AccStore<R>*)a.part_b + blockIdx.x);
+  grad_tile<R, MAT, DELTA>(a, blockIdx.x, a.st);
 }
 
 // ---------------------------------------------------------------------------
 // vertex pass
 // ---------------------------------------------------------------------------
-template <class R>
+template <class R, bool DELTA>
 __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_kernel(SolveArgs a, int use_cond) {
   constexpr int N = 12;
   __shared__ Acc<R> red[(kVThreads / 32) * N];
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
       s0 = a.off[i];
       s1 = a.off[i + 1];
     }
-    vertex_update<R>(a, i, s0, s1, t, P, s);
+    vertex_update<R, DELTA>(a, i, s0, s1, t, P, s);
   }
   double tot[N];
   // float-float block sums for the quantities whose terms change sign
@@ -277,12 +279,35 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
                             (!st->done && st->iter < st->iter_limit) ? 1u : 0u);
 }
 
-// total energy at x: gradient-pass partials + external work (on demand)
+// total energy at x, on demand: an element pass into per-tile partials, then
+// their sum plus the external work of the last vertex pass
+template <class R, int MAT>
+__global__ void __launch_bounds__(kElemThreads) solver_energy_pass_kernel(SolveArgs a) {
+  energy_tile<R, MAT>(a, blockIdx.x, (AccStore<R>*)a.part_b + blockIdx.x);
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) solver_energy_kernel(SolveArgs a) {
   __shared__ Acc<R> red[8];
   const double e = block_sum_partials<R>((const AccStore<R>*)a.part_b, a.fv.n_tiles, 1, red);
   if (threadIdx.x == 0) a.st->energy = e + a.st->ext_energy;
+}
+
+// refresh of the reference state (FP32 stable Neo-Hookean); in the iteration
+// graph both follow the vertex pass as programmatic dependents and return at
+// once unless it asked for a refresh
+__global__ void __launch_bounds__(kGradThreads) solver_ref_elem_kernel(SolveArgs a) {
+  pdl_trigger();
+  pdl_wait();
+  if (!a.st->refresh) return;
+  ref_tile(a, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kVThreads) solver_ref_vertex_kernel(SolveArgs a) {
+  pdl_trigger();
+  pdl_wait();
+  if (!a.st->refresh) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) ref_vertex(a, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -306,6 +331,12 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     ((V4<R>*)a.gd)[2 * i + 1] = z;
     ((V4<R>*)a.p0)[i] = z;
     ((V4<R>*)a.p1)[i] = z;
+    if (a.delta) {  // x_ref = 0, g(x_ref) = -f (no element stress at u = 0)
+      V4<R> f = z;
+      if (a.force) f = ((const V4<R>*)a.force)[i];
+      ((V4<R>*)a.xref)[i] = z;
+      ((V4<R>*)a.gref)[i] = V4<R>{-f.x, -f.y, -f.z, R(0)};
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     SolverState* st = a.st;
@@ -332,10 +363,14 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     st->decided = 1;
     st->error = 0;
     st->pbuf = 0;
+    st->refresh = 0;
+    st->gnorm_ref = 0.0;
   }
 }
 
 __global__ void solver_set_limit_kernel(SolverState* st, int n) { st->iter_limit = st->iter + n; }
+
+__global__ void solver_force_refresh_kernel(SolverState* st) { st->refresh = 1; }
 
 template <class R>
 __global__ void solver_unpack_kernel(int n, const V4<R>* __restrict__ xa, const int32_t* __restrict__ uoi,
@@ -353,8 +388,10 @@ template <class R>
 static cudaError_t prepare_t() {
   const int g = (int)grad_smem_bytes<R>();
   const cudaFuncAttribute m = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_ARAP>, m, g);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN>, m, g);
+  cudaError_t e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_ARAP, false>, m, g);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN, false>, m, g);
+  if (e == cudaSuccess && kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>)
+    e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>, m, g);
   return e;
 }
 
@@ -380,10 +417,21 @@ cudaError_t launch_solver_set_limit(const SolveArgs& a, int n_steps, cudaStream_
 }
 
 cudaError_t launch_solver_energy(const SolveArgs& a, cudaStream_t s) {
-  if (a.precision == AGB_F64)
+  if (a.fv.n_tiles == 0) return cudaErrorInvalidValue;
+  const int nt = a.fv.n_tiles;
+  if (a.precision == AGB_F64) {
+    if (a.fv.material == AGB_ARAP)
+      solver_energy_pass_kernel<double, AGB_ARAP><<<nt, kElemThreads, 0, s>>>(a);
+    else
+      solver_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN><<<nt, kElemThreads, 0, s>>>(a);
     solver_energy_kernel<double><<<1, 256, 0, s>>>(a);
-  else
+  } else {
+    if (a.fv.material == AGB_ARAP)
+      solver_energy_pass_kernel<float, AGB_ARAP><<<nt, kElemThreads, 0, s>>>(a);
+    else
+      solver_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN><<<nt, kElemThreads, 0, s>>>(a);
     solver_energy_kernel<float><<<1, 256, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -405,8 +453,8 @@ static cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t sme
   return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
-template <class R, int MAT>
-static cudaError_t launch_iteration_t(const SolveArgs& a, bool use_cond, bool first, int max_bt,
+template <class R, int MAT, bool DELTA>
+static cudaError_t launch_iteration_d(const SolveArgs& a, bool use_cond, bool first, int max_bt,
                                       cudaStream_t s) {
   const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
   if (!first) {
@@ -415,10 +463,21 @@ static cudaError_t launch_iteration_t(const SolveArgs& a, bool use_cond, bool fi
       for (int j0 = 0; j0 <= max_bt; j0 += 3) solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0);
     }
   }
-  cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a);
+  cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a);
   if (e != cudaSuccess) return e;
-  return launch_pdl(solver_vertex_kernel<R>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond ? 1 : 0);
+  return launch_pdl(solver_vertex_kernel<R, DELTA>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond ? 1 : 0);
 }
+
+template <class R, int MAT>
+static cudaError_t launch_iteration_t(const SolveArgs& a, bool use_cond, bool first, int max_bt,
+                                      cudaStream_t s) {
+  if (a.delta) {  // the reference-state kernels read x_ref and g(x_ref)
+    if (!kRefDelta<R, MAT> || !a.xref || !a.gref) return cudaErrorInvalidValue;
+    return launch_iteration_d<R, MAT, kRefDelta<R, MAT>>(a, use_cond, first, max_bt, s);
+  }
+  return launch_iteration_d<R, MAT, false>(a, use_cond, first, max_bt, s);
+}
+
 
 static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool first, cudaStream_t s) {
   if (a.fv.n_tiles == 0) return cudaErrorInvalidValue;
@@ -439,14 +498,22 @@ static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool firs
   return cudaGetLastError();
 }
 
-template <class R, int MAT>
-static cudaError_t launch_pass_t(const SolveArgs& a, int which, cudaStream_t s) {
+template <class R, int MAT, bool DELTA>
+static cudaError_t launch_pass_d(const SolveArgs& a, int which, cudaStream_t s) {
   const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
   if (which == 0) solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, 0);
-  if (which == 1) solver_grad_kernel<R, MAT><<<eg, kGradThreads, grad_smem_bytes<R>(), s>>>(a);
-  if (which == 2) solver_vertex_kernel<R><<<a.vblocks, kVThreads, 0, s>>>(a, 0);
+  if (which == 1) solver_grad_kernel<R, MAT, DELTA><<<eg, kGradThreads, grad_smem_bytes<R>(), s>>>(a);
+  if (which == 2) solver_vertex_kernel<R, DELTA><<<a.vblocks, kVThreads, 0, s>>>(a, 0);
   return cudaGetLastError();
 }
+
+template <class R, int MAT>
+static cudaError_t launch_pass_t(const SolveArgs& a, int which, cudaStream_t s) {
+  if (a.delta && (!kRefDelta<R, MAT> || !a.xref || !a.gref)) return cudaErrorInvalidValue;
+  if (a.delta) return launch_pass_d<R, MAT, kRefDelta<R, MAT>>(a, which, s);
+  return launch_pass_d<R, MAT, false>(a, which, s);
+}
+
 
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s) {
   if (a.precision == AGB_F64) {
@@ -474,6 +541,20 @@ cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_
   else
     solver_unpack_kernel<float><<<blocks, kVThreads, 0, s>>>(a.n_points, (const V4<float>*)a.xa, uoi,
                                                             (float*)u);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s) {
+  if (!a.delta) return cudaSuccess;
+  if (!a.xref || !a.gref || a.precision != AGB_F32 || a.fv.material != AGB_STABLE_NEO_HOOKEAN)
+    return cudaErrorInvalidValue;
+  cudaError_t e = launch_pdl(solver_ref_elem_kernel, dim3(a.fv.n_tiles), dim3(kGradThreads), ref_smem_bytes(), s, a);
+  if (e == cudaSuccess) e = launch_pdl(solver_ref_vertex_kernel, dim3(a.vblocks), dim3(kVThreads), 0, s, a);
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t launch_solver_force_refresh(const SolveArgs& a, cudaStream_t s) {
+  solver_force_refresh_kernel<<<1, 1, 0, s>>>(a.st);
   return cudaGetLastError();
 }
 

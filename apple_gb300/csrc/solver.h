@@ -41,6 +41,11 @@ struct SolverState {
   int32_t decided;     // ARAP: a trial pass has decided the step
   int32_t error;       // device-side status (nonzero = a guard tripped)
   int32_t pbuf;        // p[pbuf] holds p_prev; the direction pass writes p into p[pbuf ^ 1]
+  // reference-state correction (FP32 stable Neo-Hookean): refresh x_ref and
+  // g(x_ref) once ||g|| has dropped by ref_ratio since the last refresh
+  int32_t refresh;     // the refresh passes run after this iteration's vertex pass
+  double gnorm_ref;    // ||g|| at the last refresh
+  double ref_ratio;    // 0: off
 };
 
 // Everything a solver kernel needs, by value.
@@ -56,6 +61,13 @@ struct SolveArgs {
   void* gd;
   void* p0;
   void* p1;
+  // reference state (delta != 0): xref[v] = (x_ref, 0) and gref[v] = the
+  // gradient at x_ref computed in FP64 (external force folded in), rounded
+  // once to R; the gradient pass then evaluates only f_e(x) - f_e(x_ref),
+  // which FP32 resolves to its own relative precision
+  void* xref;
+  void* gref;
+  int delta;
   const void* force;  // V4<R> external force per vertex or null
   const int32_t* slot_of_tv;
   const int32_t* off;  // CSR over slots (n_points + 1)
@@ -64,7 +76,7 @@ struct SolveArgs {
   SolverState* st;
   void* part_a;        // direction-pass partials (n_tiles x 6) and group partials
   void* gpart_a;
-  void* part_b;        // gradient-pass energy partials (n_tiles x 1)
+  void* part_b;        // energy partials of the on-demand energy pass (n_tiles x 1)
   void* part_v;        // vertex-pass partials (vblocks x 12) and group partials
   void* gpart_v;
   void* part_t;        // ARAP trial partials (n_tiles x 3) and group partials
@@ -90,11 +102,17 @@ int solver_vertex_blocks(int n_points);
 // set kernel attributes (dynamic shared memory of the gradient pass); call
 // once before launching or capturing solver kernels
 cudaError_t solver_prepare_kernels(int precision);
-// sum the gradient pass's energy partials and the external work into st->energy
+// energy at x into st->energy: an element pass (per-tile partials) and their
+// sum plus the external work of the last vertex pass
 cudaError_t launch_solver_energy(const SolveArgs& a, cudaStream_t s);
 size_t solver_grad_smem(int precision);
 // one pass of an iteration on its own: 0 direction, 1 gradient, 2 vertex
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s);
+// the refresh of the reference state (element pass in FP64, vertex pass);
+// both return at once unless st->refresh is set
+cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s);
+// set st->refresh (the next refresh passes run unconditionally)
+cudaError_t launch_solver_force_refresh(const SolveArgs& a, cudaStream_t s);
 
 // Adjoint CG (adjoint.cu): scalars of H lam = rhs on the free DOFs at the
 // solver's current x, kept on the device like SolverState.
@@ -148,7 +166,7 @@ struct BatchArgs {
   SolverState* st;             // n_meshes
   BatchState* bs;
   void* part_dir;              // n_tiles x 6
-  void* part_grad;             // n_tiles
+  void* part_grad;             // n_tiles energy partials (on demand)
   void* part_vert;             // n_chunks x 12
   unsigned long long cond;
 };
@@ -200,6 +218,8 @@ struct agb_solver {
   void* d_gd = nullptr;
   void* d_p0 = nullptr;
   void* d_p1 = nullptr;
+  void* d_xref = nullptr;  // reference state (FP32 stable Neo-Hookean)
+  void* d_gref = nullptr;
   void* d_slots = nullptr;
   void* d_part = nullptr;
   unsigned* d_cnt = nullptr;

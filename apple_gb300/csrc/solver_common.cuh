@@ -271,13 +271,20 @@ __device__ __forceinline__ void vertex_decide(SolverState* st, const double* tot
   if (result != AGB_RUNNING) {
     st->done = 1;
     st->result = result;
+  } else if (st->ref_ratio > 0.0) {
+    if (first)
+      st->gnorm_ref = gnorm;
+    else if (gnorm <= st->ref_ratio * st->gnorm_ref) {
+      st->refresh = 1;
+      st->gnorm_ref = gnorm;
+    }
   }
 }
 
 // One vertex of the vertex pass: x <- x + t p (float-float), g and d from the
 // vertex's slots s0..s1 (fixed order), external force, DOF mask; the 12 sums
 // of vertex_decide accumulate into s.
-template <class R>
+template <class R, bool DELTA>
 __device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0, int s1, R t, const V4<R>* P,
                                               R (&s)[12]) {
   V4<R>* XA = (V4<R>*)a.xa;
@@ -301,7 +308,17 @@ __device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0,
     ds[1] += sd.y;
     ds[2] += sd.z;
   }
-  if (F) {
+  if constexpr (DELTA) {
+    // g = g(x_ref) + sum_e (f_e(x) - f_e(x_ref)); the force is folded into g(x_ref)
+    const V4<R> r = ldg4((const V4<R>*)a.gref + i);
+    gs[0] += r.x;
+    gs[1] += r.y;
+    gs[2] += r.z;
+    if (F) {
+      const V4<R> f = ldg4(F + i);
+      s[11] += -(f.x * xn[0] + f.y * xn[1] + f.z * xn[2]);
+    }
+  } else if (F) {
     const V4<R> f = ldg4(F + i);
     gs[0] -= f.x;
     gs[1] -= f.y;
@@ -340,21 +357,73 @@ __device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0,
   GD[2 * i + 1] = V4<R>{dn[0], dn[1], dn[2], R(0)};
 }
 
+// Whether a solver instantiation uses the reference-state correction: FP32
+// stable Neo-Hookean (FP64 has the precision; ARAP is not polynomial).
+template <class R, int MAT>
+constexpr bool kRefDelta = MAT == AGB_STABLE_NEO_HOOKEAN && sizeof(R) == 4;
+
+// x + t p relative to the reference: (x_ref, d.x) and (d.y, d.z) per vertex,
+// d = (x_hi + t p - x_ref) + x_lo with the hi/lo pair updated by two-sum
+template <class R>
+__device__ __forceinline__ void stage_point_delta(const SolveArgs& a, const int (&vid)[kGradVerts], const V4<R>* P,
+                                                  R t, V4<R>* sh, V2<R>* sl) {
+  const V4<R>* XA = (const V4<R>*)a.xa;
+  const V4<R>* XR = (const V4<R>*)a.xref;
+#pragma unroll
+  for (int j = 0; j < kGradVerts; ++j) {
+    const int v = vid[j], i = threadIdx.x + j * kGradThreads;
+    if (v < 0) continue;
+    const V4<R> x = ldg4(XA + 2 * v), xl = ldg4(XA + 2 * v + 1), p = ldg4(P + v), r = ldg4(XR + v);
+    R hx = x.x, lx = xl.x, hy = x.y, ly = xl.y, hz = x.z, lz = xl.z;
+    pair_add(hx, lx, mul_rn(t, p.x));
+    pair_add(hy, ly, mul_rn(t, p.y));
+    pair_add(hz, lz, mul_rn(t, p.z));
+    sh[i] = V4<R>{r.x, r.y, r.z, add_rn(sub_rn(hx, r.x), lx)};
+    sl[i] = V2<R>{add_rn(sub_rn(hy, r.y), ly), add_rn(sub_rn(hz, r.z), lz)};
+  }
+}
+
+// A = grad of x_ref, dG = grad of d from the delta staging
+template <class R>
+__device__ __forceinline__ void delta_gradient(const V4<R>* sh, const V2<R>* sl, const int (&l)[4],
+                                               const R (&D)[3][3], R (&A)[3][3], R (&dG)[3][3]) {
+  const V4<R> h0 = sh[l[0]];
+  const V2<R> q0 = sl[l[0]];
+  R ea[3][3], ed[3][3];
+#pragma unroll
+  for (int k = 1; k < 4; ++k) {
+    const V4<R> h = sh[l[k]];
+    const V2<R> q = sl[l[k]];
+    ea[0][k - 1] = h.x - h0.x;
+    ea[1][k - 1] = h.y - h0.y;
+    ea[2][k - 1] = h.z - h0.z;
+    ed[0][k - 1] = h.w - h0.w;
+    ed[1][k - 1] = q.x - q0.x;
+    ed[2][k - 1] = q.y - q0.y;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      A[i][j] = ea[i][0] * D[0][j] + ea[i][1] * D[1][j] + ea[i][2] * D[2][j];
+      dG[i][j] = ed[i][0] * D[0][j] + ed[i][1] * D[1][j] + ed[i][2] * D[2][j];
+    }
+}
+
 // The gradient pass over one tile (one CTA of kGradThreads threads, dynamic
-// shared memory grad_smem_bytes<R>()): stage x + t p, per warp group energy,
-// forces and clamped diagonal into the warp's private accumulator, then one
-// slot per tile vertex and the tile's energy partial.  st is the state of
+// shared memory grad_smem_bytes<R>()): stage x + t p, per warp group forces
+// and clamped diagonal into the warp's private accumulator, then one slot per
+// tile vertex.  (The energy is not needed by the iteration; energy_tile
+// evaluates it on demand.)  st is the state of
 // the tile's mesh; the first group's record, the vertex ids and the slot
 // indices are read before the dependency wait.
-template <class R, int MAT>
-__device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const SolverState* st,
-                                          AccStore<R>* energy_out) {
+template <class R, int MAT, bool DELTA = kRefDelta<R, MAT>>
+__device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const SolverState* st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V4<R>* sh = reinterpret_cast<V4<R>*>(smem_raw);
   V4<R>* acc4 = sh + kTileVerts;  // [warp][vertex]: gx gy gz dx
   V2<R>* sl = reinterpret_cast<V2<R>*>(acc4 + kGradWarps * kTileVerts);
   V2<R>* acc2 = sl + kTileVerts;  // [warp][vertex]: dy dz
-  __shared__ Acc<R> red[kGradWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gs = a.fv.tile_gstart[tile], ge = a.fv.tile_gstart[tile + 1];
   // constant inputs: the first group's element record
@@ -378,7 +447,10 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
   pdl_trigger();
   pdl_wait();
   if (st->done) return;
-  stage_point<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
+  if constexpr (DELTA)
+    stage_point_delta<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
+  else
+    stage_point<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
   for (int i = threadIdx.x; i < kGradWarps * kTileVerts; i += blockDim.x) {
     acc4[i] = V4<R>{R(0), R(0), R(0), R(0)};
     acc2[i] = V2<R>{R(0), R(0)};
@@ -387,7 +459,6 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
 
   V4<R>* my4 = acc4 + warp * kTileVerts;
   V2<R>* my2 = acc2 + warp * kTileVerts;
-  Acc<R> sums[1] = {};
   while (g < ge) {
     // prefetch the warp's next group while this one computes
     const int gn = g + kGradWarps;
@@ -403,19 +474,27 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
     R f[4][3], hd[4][3];
     if (lane < n) {
       R G[3][3], P[3][3];
-      pair_gradient(sh, sl, l, geo.D, G);
-      if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      if constexpr (DELTA) {
+        // f_e(x) - f_e(x_ref) from P(A + dG) - P(A); energy and diagonal at A + dG
+        R dG[3][3];
+        delta_gradient(sh, sl, l, geo.D, G, dG);
+        SnhPoint<R> s, s2;
+        snh_prepare(G, s);
+        snh_pk1_delta(s, dG, geo.mu, geo.lam, P, s2);
+        corner_vjp(P, geo.D, f);
+        snh_hess_diag(s2, geo.D, geo.mu, geo.lam, hd);
+      } else if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+        pair_gradient(sh, sl, l, geo.D, G);
         SnhPoint<R> s;
         snh_prepare(G, s);
-        sums[0].add(snh_energy(s, geo.mu, geo.lam));
         snh_pk1(s, geo.mu, geo.lam, P);
         corner_vjp(P, geo.D, f);
         snh_hess_diag(s, geo.D, geo.mu, geo.lam, hd);
       } else {
+        pair_gradient(sh, sl, l, geo.D, G);
         const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
         Svd<R> sv;
         svd_rv(G, jm1, sv);
-        sums[0].add(arap_energy(sv, geo.mu));
         arap_pk1(sv, geo.mu, P);
         corner_vjp(P, geo.D, f);
         R lk[3];
@@ -468,8 +547,154 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
     slots[2 * sidx[j]] = V4<R>{q4.x, q4.y, q4.z, R(0)};
     slots[2 * sidx[j] + 1] = V4<R>{q4.w, q2.x, q2.y, R(0)};
   }
-  block_reduce<1, 0x0u, R>(sums, red);
-  if (threadIdx.x == 0) *energy_out = acc_store(sums[0]);
+}
+
+// ---------------------------------------------------------------------------
+// refresh of the reference state: x_ref = x_hi, and g(x_ref) = sum_e f_e(x_ref)
+// - f_ext with the FP32 element data in FP64 arithmetic, stored as a float
+// pair.  The element pass runs one CTA per tile (kGradThreads threads, warp
+// groups, per-warp FP64 accumulators) and writes each tile vertex's sum as
+// three doubles into its 32-byte slot; the vertex pass adds the slots.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr size_t ref_smem_bytes() {
+  return (size_t)kTileVerts * (size_t)(kGradWarps + 1) * sizeof(V4<double>);
+}
+
+__device__ __forceinline__ void ref_tile(const SolveArgs& a, int tile) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V4<double>* sx = reinterpret_cast<V4<double>*>(smem_raw);
+  V4<double>* acc = sx + kTileVerts;  // [warp][vertex]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  const V4<float>* XA = (const V4<float>*)a.xa;
+  V4<float>* XR = (V4<float>*)a.xref;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const int v = a.fv.tv_vid[vs + i];
+    const V4<float> x = XA[2 * v];
+    XR[v] = V4<float>{x.x, x.y, x.z, 0.f};  // tiles sharing v store equal values
+    sx[i] = V4<double>{(double)x.x, (double)x.y, (double)x.z, 0.0};
+  }
+  for (int i = threadIdx.x; i < kGradWarps * kTileVerts; i += blockDim.x) acc[i] = V4<double>{0.0, 0.0, 0.0, 0.0};
+  __syncthreads();
+  V4<double>* my = acc + warp * kTileVerts;
+  for (int g = a.fv.tile_gstart[tile] + warp; g < a.fv.tile_gstart[tile + 1]; g += kGradWarps) {
+    const int e0 = a.fv.group_estart[g], n = a.fv.group_estart[g + 1] - e0;
+    double f[4][3] = {};
+    int l[4] = {0, 0, 0, 0};
+    if (lane < n) {
+      ElemGeo<float> gf;
+      uint32_t ids;
+      load_elem<float>(a.fv, e0 + lane, gf, ids);
+      ElemGeo<double> geo;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) geo.D[i][j] = (double)gf.D[i][j];
+      geo.mu = (double)gf.mu;
+      geo.lam = (double)gf.lam;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) l[k] = corner(ids, k);
+      double G[3][3], P[3][3];
+      vec_gradient(sx, l, geo.D, G);
+      SnhPoint<double> s;
+      snh_prepare(G, s);
+      snh_pk1(s, geo.mu, geo.lam, P);
+      corner_vjp(P, geo.D, f);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      __syncwarp();
+      if (lane < n) {
+        V4<double> q = my[l[k]];
+        q.x += f[k][0];
+        q.y += f[k][1];
+        q.z += f[k][2];
+        my[l[k]] = q;
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  double* slots = (double*)a.slots;  // 4 doubles per 32-byte slot
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    V4<double> q = acc[i];
+#pragma unroll
+    for (int w = 1; w < kGradWarps; ++w) {
+      const V4<double> r = acc[w * kTileVerts + i];
+      q.x += r.x;
+      q.y += r.y;
+      q.z += r.z;
+    }
+    const size_t k = 4 * (size_t)a.slot_of_tv[vs + i];
+    slots[k] = q.x;
+    slots[k + 1] = q.y;
+    slots[k + 2] = q.z;
+  }
+}
+
+__device__ __forceinline__ void ref_vertex(const SolveArgs& a, int i) {
+  const double* slots = (const double*)a.slots;
+  double g[3] = {0.0, 0.0, 0.0};
+  for (int k = a.off[i]; k < a.off[i + 1]; ++k) {
+    g[0] += slots[4 * (size_t)k];
+    g[1] += slots[4 * (size_t)k + 1];
+    g[2] += slots[4 * (size_t)k + 2];
+  }
+  if (a.force) {
+    const V4<float> f = ((const V4<float>*)a.force)[i];
+    g[0] -= (double)f.x;
+    g[1] -= (double)f.y;
+    g[2] -= (double)f.z;
+  }
+  // one float suffices: g(x_ref) is itself a residual (at most 1/ref_ratio
+  // times the current one), so its rounding is far below the current ||g||
+  const V4<float> gr{(float)g[0], (float)g[1], (float)g[2], 0.f};
+  ((V4<float>*)a.gref)[i] = gr;
+  // the stored g of this iterate becomes the new reference's value too
+  // (x_ref = x_hi differs from x by x_lo only), so the next y = g - g_prev
+  // of the Dai-Kou beta does not see the change of reference
+  const int mask = (int)((const V4<float>*)a.xa)[2 * i].w;
+  ((V4<float>*)a.gd)[2 * i] = V4<float>{(mask & 1) ? 0.f : gr.x, (mask & 2) ? 0.f : gr.y, (mask & 4) ? 0.f : gr.z, 0.f};
+}
+
+// Energy at x (no line-search offset), one CTA of kElemThreads threads per
+// tile: sum of Psi_e dV_e over the tile's elements into `out` (the reporting
+// energy of the solver; FP32 element math, float-float block sum).
+template <class R, int MAT>
+__device__ __forceinline__ void energy_tile(const SolveArgs& a, int tile, AccStore<R>* out) {
+  __shared__ V4<R> sh[kTileVerts];
+  __shared__ V2<R> sl[kTileVerts];
+  __shared__ Acc<R> red[kElemThreads / 32];
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  const V4<R>* XA = (const V4<R>*)a.xa;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const int v = a.fv.tv_vid[vs + i];
+    const V4<R> x = XA[2 * v], xl = XA[2 * v + 1];
+    sh[i] = V4<R>{x.x, x.y, x.z, xl.x};
+    sl[i] = V2<R>{xl.y, xl.z};
+  }
+  __syncthreads();
+  Acc<R> sums[1] = {};
+  for (int e = a.fv.tile_estart[tile] + threadIdx.x; e < a.fv.tile_estart[tile + 1]; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem<R>(a.fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R G[3][3];
+    pair_gradient(sh, sl, l, geo.D, G);
+    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      SnhPoint<R> s;
+      snh_prepare(G, s);
+      sums[0].add(snh_energy(s, geo.mu, geo.lam));
+    } else {
+      const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
+      Svd<R> sv;
+      svd_rv(G, jm1, sv);
+      sums[0].add(arap_energy(sv, geo.mu));
+    }
+  }
+  block_reduce<1, 0xffffffffu, R>(sums, red);
+  if (threadIdx.x == 0) *out = acc_store(sums[0]);
 }
 
 }  // namespace agb

@@ -163,10 +163,14 @@ class DeviceSolver:
 
 class PNCG:
     def __init__(self, criteria: ConvergenceCriteria | None = None, line_search: LineSearch | None = None,
-                 *, beta_max: float = 10.0):
+                 *, beta_max: float = 10.0, refresh_ratio: float = -1.0):
         self.criteria = criteria or ConvergenceCriteria()
         self.line_search = line_search or LineSearch()
         self.beta_max = beta_max
+        # FP32 stable Neo-Hookean reference-state correction: refresh the FP64
+        # reference gradient each time ||g|| drops by this factor; 0: off;
+        # < 0: on (1e-2) when rtol < 1e-5 asks for more than FP32 forces resolve
+        self.refresh_ratio = refresh_ratio
         self._solvers: dict[int, DeviceSolver] = {}
 
     def params(self, dtype) -> _lib.PncgParams:
@@ -182,6 +186,7 @@ class PNCG:
         p.armijo_c = float(self.line_search.c)
         p.overstep = float(self.line_search.overstep)
         p.beta_max = float(self.beta_max)
+        p.refresh_ratio = float(self.refresh_ratio)
         return p
 
     def solver(self, problem) -> DeviceSolver:
