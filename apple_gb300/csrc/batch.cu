@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs 
   pdl_wait();
   SolverState* st = b.st + blockIdx.x;
   if (st->done) return;
+  if (threadIdx.x == 0) st->refresh = 0;  // the refresh passes, if any, ran after the last vertex tail
   const int t0 = b.mesh_tile0[blockIdx.x], t1 = b.mesh_tile0[blockIdx.x + 1];
   Acc<R> s[N] = {};
   for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
@@ -95,12 +96,12 @@ __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs 
   }
 }
 
-template <class R>
+template <class R, bool DELTA>
 __global__ void __launch_bounds__(kGradThreads, 7) batch_grad_kernel(BatchArgs b) {
-  grad_tile<R, AGB_STABLE_NEO_HOOKEAN, false>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
+  grad_tile<R, AGB_STABLE_NEO_HOOKEAN, DELTA>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
 }
 
-template <class R>
+template <class R, bool DELTA>
 __global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
   constexpr int N = 12;
   constexpr unsigned FF = (1u << 1) | (1u << 6) | (1u << 8) | (1u << 9);
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
   const R t = (R)st->t;
   const V4<R>* P = p_cur<R>(a, st->pbuf);
   R s[N] = {};
-  for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) vertex_update<R, false>(a, i, a.off[i], a.off[i + 1], t, P, s);
+  for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) vertex_update<R, DELTA>(a, i, a.off[i], a.off[i + 1], t, P, s);
   Acc<R> acc[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) {
@@ -170,6 +171,26 @@ __global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchAr
                             (active > 0u && bs->iter < bs->iter_limit) ? 1u : 0u);
 }
 
+// reference-state refresh of the models that asked for one (FP32)
+__global__ void __launch_bounds__(kGradThreads) batch_ref_elem_kernel(BatchArgs b) {
+  pdl_trigger();
+  pdl_wait();
+  if (!b.st[b.tile_mesh[blockIdx.x]].refresh) return;
+  ref_tile(b.a, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kVThreads) batch_ref_vertex_kernel(BatchArgs b) {
+  pdl_trigger();
+  pdl_wait();
+  const int c = blockIdx.x;
+  if (!b.st[b.chunk_mesh[c]].refresh) return;
+  for (int i = b.chunk_v0[c] + threadIdx.x; i < b.chunk_v0[c + 1]; i += blockDim.x) ref_vertex(b.a, i);
+}
+
+__global__ void batch_force_refresh_kernel(BatchArgs b) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < b.n_meshes; m += gridDim.x * blockDim.x) b.st[m].refresh = 1;
+}
+
 template <class R>
 __global__ void __launch_bounds__(kElemThreads) batch_energy_pass_kernel(BatchArgs b) {
   energy_tile<R, AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x, (AccStore<R>*)b.part_grad + blockIdx.x);
@@ -202,6 +223,10 @@ __global__ void batch_init_vertex_kernel(BatchArgs b, const R* __restrict__ u, c
     ((V4<R>*)a.gd)[2 * i + 1] = z;
     ((V4<R>*)a.p0)[i] = z;
     ((V4<R>*)a.p1)[i] = z;
+    if (a.delta) {
+      ((V4<R>*)a.xref)[i] = z;
+      ((V4<R>*)a.gref)[i] = z;
+    }
   }
 }
 
@@ -220,6 +245,8 @@ __global__ void batch_init_state_kernel(BatchArgs b, SolverState proto) {
     st.decided = 1;
     st.error = 0;
     st.pbuf = 0;
+    st.refresh = 0;
+    st.gnorm_ref = 0.0;
     b.st[m] = st;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *b.bs = BatchState{0, 0, 0u, 0u};
@@ -242,14 +269,30 @@ cudaError_t launch_pdl_b(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cu
   return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
-template <class R>
-cudaError_t batch_grad_and_vertex(const BatchArgs& b, cudaStream_t s) {
-  cudaError_t e = launch_pdl_b(batch_grad_kernel<R>, dim3(b.a.fv.n_tiles), dim3(kGradThreads),
+cudaError_t batch_refresh(const BatchArgs& b, cudaStream_t s) {
+  cudaError_t e = launch_pdl_b(batch_ref_elem_kernel, dim3(b.a.fv.n_tiles), dim3(kGradThreads), ref_smem_bytes(), s, b);
+  if (e == cudaSuccess) e = launch_pdl_b(batch_ref_vertex_kernel, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
+  return e;
+}
+
+template <class R, bool DELTA>
+cudaError_t batch_grad_and_vertex_d(const BatchArgs& b, cudaStream_t s) {
+  cudaError_t e = launch_pdl_b(batch_grad_kernel<R, DELTA>, dim3(b.a.fv.n_tiles), dim3(kGradThreads),
                                grad_smem_bytes<R>(), s, b);
-  if (e == cudaSuccess) e = launch_pdl_b(batch_vertex_kernel<R>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
+  if (e == cudaSuccess) e = launch_pdl_b(batch_vertex_kernel<R, DELTA>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
   if (e == cudaSuccess)
     e = launch_pdl_b(batch_vertex_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  if (e == cudaSuccess && DELTA) e = batch_refresh(b, s);
   return e;
+}
+
+template <class R>
+cudaError_t batch_grad_and_vertex(const BatchArgs& b, cudaStream_t s) {
+  if (b.a.delta) {
+    if (!kRefDelta<R, AGB_STABLE_NEO_HOOKEAN> || !b.a.xref || !b.a.gref) return cudaErrorInvalidValue;
+    return batch_grad_and_vertex_d<R, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>(b, s);
+  }
+  return batch_grad_and_vertex_d<R, false>(b, s);
 }
 
 template <class R>
@@ -263,8 +306,11 @@ cudaError_t batch_iteration_t(const BatchArgs& b, cudaStream_t s) {
 
 template <class R>
 cudaError_t batch_prepare_t() {
-  return cudaFuncSetAttribute(batch_grad_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)grad_smem_bytes<R>());
+  const cudaFuncAttribute m = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(batch_grad_kernel<R, false>, m, (int)grad_smem_bytes<R>());
+  if (e == cudaSuccess && kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>)
+    e = cudaFuncSetAttribute(batch_grad_kernel<R, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>, m, (int)grad_smem_bytes<R>());
+  return e;
 }
 
 }  // namespace
@@ -293,6 +339,11 @@ cudaError_t launch_batch_iteration(const BatchArgs& b, cudaStream_t s) {
 
 cudaError_t launch_batch_first(const BatchArgs& b, cudaStream_t s) {
   if (b.a.fv.n_tiles == 0 || b.n_meshes == 0) return cudaErrorInvalidValue;
+  if (b.a.delta) {  // x_ref = x_0 and g(x_0) in FP64 for every model
+    batch_force_refresh_kernel<<<(b.n_meshes + 255) / 256, 256, 0, s>>>(b);
+    const cudaError_t e = batch_refresh(b, s);
+    if (e != cudaSuccess) return e;
+  }
   const cudaError_t e =
       b.a.precision == AGB_F64 ? batch_grad_and_vertex<double>(b, s) : batch_grad_and_vertex<float>(b, s);
   return e != cudaSuccess ? e : cudaGetLastError();

@@ -1007,7 +1007,8 @@ int agb_batch_destroy(agb_batch* b) {
                   (void*)b->d_group_estart, (void*)b->d_tv_vid, b->d_rec, (void*)b->d_ids,
                   (void*)b->d_slot_of_tv, (void*)b->d_off, (void*)b->d_uoi, b->d_fixed, b->d_force,
                   (void*)b->d_tile_mesh, (void*)b->d_mesh_tile0, (void*)b->d_chunk_v0, (void*)b->d_chunk_mesh,
-                  (void*)b->d_mesh_chunk0, b->d_xa, b->d_gd, b->d_p0, b->d_p1, b->d_slots, b->d_part,
+                  (void*)b->d_mesh_chunk0, b->d_xa, b->d_gd, b->d_p0, b->d_p1, b->d_xref, b->d_gref, b->d_slots,
+                  b->d_part,
                   (void*)b->d_state, (void*)b->d_bstate})
     dfree(p);
   if (b->h_state) cudaFreeHost(b->h_state);
@@ -1034,6 +1035,9 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   AGB_REQUIRE(prm.max_steps >= 0 && prm.max_backtracking >= 0 && prm.max_backtracking <= 60, AGB_E_INVALID,
               "agb_batch_create: bad parameters");
   if (chunk_verts <= 0) chunk_verts = 512;
+  AGB_REQUIRE(prm.refresh_ratio < 1.0, AGB_E_INVALID, "agb_batch_create: bad parameters");
+  if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-2 : 0.0;
+  const bool delta = prec == AGB_F32 && prm.refresh_ratio > 0.0;
   agb_batch* b = new (std::nothrow) agb_batch();
   AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_create: out of host memory");
   b->models.assign(models, models + n_models);
@@ -1145,6 +1149,8 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   if (!rc) rc = dalloc_bytes(&b->d_gd, 2 * v4 * np);
   if (!rc) rc = dalloc_bytes(&b->d_p0, v4 * np);
   if (!rc) rc = dalloc_bytes(&b->d_p1, v4 * np);
+  if (!rc && delta) rc = dalloc_bytes(&b->d_xref, v4 * np);
+  if (!rc && delta) rc = dalloc_bytes(&b->d_gref, v4 * np);
   if (!rc) rc = dalloc_bytes(&b->d_slots, 2 * v4 * (size_t)b->n_slots);
   const size_t n_part = (size_t)P.n_tiles * 7 + (size_t)n_chunks * 12;
   if (!rc) rc = dalloc_bytes(&b->d_part, 8 * n_part);
@@ -1176,6 +1182,9 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   a.gd = b->d_gd;
   a.p0 = b->d_p0;
   a.p1 = b->d_p1;
+  a.xref = b->d_xref;
+  a.gref = b->d_gref;
+  a.delta = delta ? 1 : 0;
   a.force = b->d_force;
   a.slot_of_tv = b->d_slot_of_tv;
   a.off = b->d_off;
@@ -1227,6 +1236,7 @@ int agb_batch_reset(agb_batch* b, const void* u, void* stream) {
   proto.beta_max = b->params.beta_max;
   proto.max_steps = b->params.max_steps;
   proto.max_bt = b->params.max_backtracking;
+  proto.ref_ratio = b->args.a.delta ? b->params.refresh_ratio : 0.0;
   RC(check_launch(launch_batch_init(b->args, u, b->d_fixed, b->d_uoi, proto, s), "batch_init"));
   RC(check_launch(launch_batch_first(b->args, s), "batch_first"));
   return AGB_OK;

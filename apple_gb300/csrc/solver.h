@@ -271,6 +271,8 @@ struct agb_batch {
   void* d_gd = nullptr;
   void* d_p0 = nullptr;
   void* d_p1 = nullptr;
+  void* d_xref = nullptr;  // reference state (FP32)
+  void* d_gref = nullptr;
   void* d_slots = nullptr;
   void* d_part = nullptr;
   agb::SolverState* d_state = nullptr;

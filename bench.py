@@ -491,7 +491,8 @@ def run_batched(a) -> None:
     n = 24 if a.small else a.n_meshes
     dims = (4, 12) if a.small else (4, 40)
     rng = np.random.default_rng(0)
-    cases = [meshgen.batch_case(k, rng, dims=dims, h=1.0 / 40) for k in range(n)]
+    # 2.5 mm cells: objects of 1-10 cm, so gravity strains of E = 1e3..1e5 Pa stay moderate
+    cases = [meshgen.batch_case(k, rng, dims=dims, h=1.0 / 400) for k in range(n)]
     crit = ag.ConvergenceCriteria(max_steps=50000, rtol=1e-6)
     dtype = torch.float32
     t0 = time.perf_counter()

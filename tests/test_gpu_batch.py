@@ -1,8 +1,9 @@
 """Batched PNCG (agb_batch_*) against the plain per-model solve and the FP64
 oracle (GB300).  Each model of the batch must converge to the displacement
 its own Forward.step() gives: the iteration is the same, only the reduction
-order differs.  Bars: FP64 1e-7 of the bounding-box diagonal vs the plain
-solve and vs the oracle; FP32 1e-4 of the diagonal vs the FP64 oracle."""
+order differs.  Bars: FP64 (rtol 1e-10) 1e-7 of the bounding-box diagonal vs
+the plain solve and vs the oracle; FP32 (rtol 1e-6, with the reference-state
+correction) 1e-5 of the diagonal."""
 
 import numpy as np
 import pytest
@@ -41,7 +42,7 @@ def _diag(m):
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_batch_matches_plain_and_oracle(cuda_device, dtype):
     cases = _cases(7)
-    rtol = 1e-10 if dtype == torch.float64 else 1e-5
+    rtol = 1e-10 if dtype == torch.float64 else 1e-6
     crit = ag.ConvergenceCriteria(max_steps=20000, rtol=rtol)
     models = [_model(m, f, dtype) for m, f in cases]
     bf = BatchedForward(models, ag.PNCG(crit))
@@ -65,8 +66,8 @@ def test_batch_matches_plain_and_oracle(cuda_device, dtype):
             assert err_plain < 1e-7 * d, (k, err_plain)
             assert err_ora < 1e-7 * d, (k, err_ora)
         else:
-            assert err_plain < 1e-4 * d, (k, err_plain)
-            assert err_ora < 1e-4 * d, (k, err_ora)
+            assert err_plain < 1e-5 * d, (k, err_plain)
+            assert err_ora < 1e-5 * d, (k, err_ora)
         assert sol.n_steps > 0
 
 
