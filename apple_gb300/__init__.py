@@ -5,7 +5,7 @@ Host side in Python (this package) over hand-written sm_103a CUDA kernels in
 """
 
 from . import meshgen
-from .fem import Arap, Space, StableNeoHookean, WarpPotentialFem, with_lame
+from .fem import Arap, Space, StableNeoHookean, StableNeoHookeanMuscle, WarpPotentialFem, with_lame
 from .forward import Forward, ForwardProblem, ModelState
 from .model import DofMap, DofMapBuilder, Model, ModelBuilder, WarpModel
 from .pncg import PNCG, ConvergenceCriteria, LineSearch, Result, Solution
@@ -30,6 +30,7 @@ __all__ = [
     "Solution",
     "Space",
     "StableNeoHookean",
+    "StableNeoHookeanMuscle",
     "WarpModel",
     "WarpPotentialFem",
     "meshgen",

@@ -15,7 +15,7 @@ LIB_PATH = pathlib.Path(__file__).resolve().parent / "libapple_gb300.so"
 
 OK = 0
 F32, F64 = 0, 1
-ARAP, STABLE_NEO_HOOKEAN = 0, 1
+ARAP, STABLE_NEO_HOOKEAN, STABLE_NEO_HOOKEAN_MUSCLE = 0, 1, 2
 FUN, GRAD, HESS_DIAG, HESS_PROD, HESS_QUAD = 1, 2, 4, 8, 16
 PRIMARY_SUCCESS, MAX_STEPS_REACHED, LINE_SEARCH_FAILED, NAN_ENCOUNTERED, RUNNING = range(5)
 
@@ -73,6 +73,7 @@ _SIGNATURES = {
     ),
     "agb_fem_destroy": (c_int, [c_void_p]),
     "agb_fem_info": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
+    "agb_fem_cells": (c_int, [c_void_p, c_void_p, POINTER(ctypes.c_uint32)]),
     "agb_fem_fun": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_hess_diag": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -111,6 +112,8 @@ _SIGNATURES = {
     "agb_cg_default_params": (None, [POINTER(CgParams)]),
     "agb_solver_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(CgParams), POINTER(CgStats), c_void_p]),
     "agb_fem_grad_param_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "agb_fem_set_activation": (c_int, [c_void_p, c_void_p]),
+    "agb_fem_grad_activation_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -11,7 +11,9 @@ Here the CG runs on the device inside the PNCG solver that produced u*
 (``DeviceSolver.adjoint`` -> ``agb_solver_adjoint``) and the pull-back is
 ``WarpPotentialFem.grad_param_vjp`` (``agb_fem_grad_param_vjp``).
 :class:`MaterialEquilibrium` packages forward + adjoint for one FEM potential
-whose per-cell ``mu`` (and ``lambda``) are the parameters, and
+whose per-cell ``mu`` (and ``lambda``) are the parameters -- and, for
+:class:`StableNeoHookeanMuscle`, the per-cell ``activation`` (the parameter
+of the reference's inverse activation fits) -- and
 :class:`EquilibriumFunction` exposes it to ``torch.autograd``.
 """
 
@@ -24,7 +26,7 @@ import numpy as np
 import torch
 
 from . import meshgen
-from .fem import StableNeoHookean, WarpPotentialFem
+from .fem import StableNeoHookean, StableNeoHookeanMuscle, WarpPotentialFem
 from .forward import Forward
 from .model import ModelBuilder
 from .pncg import PNCG, CgSolution, ConvergenceCriteria, Result, Solution
@@ -62,7 +64,9 @@ class MaterialEquilibrium:
         self.cg_rtol = cg_rtol
         self.cg_max_iter = cg_max_iter
         self.device = torch.device(device)
-        self._state = None  # (potential, solver, u*) of the last forward
+        self._state = None  # (potential, solver, u*, model) of the last forward
+        self._opt = None
+        self._key = None  # the (mu, lambda) the resident model was built with
         self.stats: AdjointStats | None = None
         self.timings: dict[str, float] = {}  # seconds of the last solve() / vjp() phases
 
@@ -70,13 +74,45 @@ class MaterialEquilibrium:
     def n_cells(self) -> int:
         return self.cells.shape[0]
 
-    def solve(self, mu, lam=None) -> torch.Tensor:
-        """Forward: the converged displacement (n_points, 3) for these cell materials."""
+    @property
+    def muscle(self) -> bool:
+        return issubclass(self.material, StableNeoHookeanMuscle)
+
+    def solve(self, mu, lam=None, activation=None) -> torch.Tensor:
+        """Forward: the converged displacement (n_points, 3) for these cell
+        materials (``activation`` (n_cells, 6): muscle only).  When only the
+        activation changed since the last call, the resident device model is
+        kept (new activation records, same tiles and solver) and the solve
+        restarts from zero free displacement."""
         t0 = time.perf_counter()
+        act = None
+        if self.muscle:
+            act = np.zeros((self.n_cells, 6)) if activation is None else \
+                np.asarray(torch.as_tensor(activation).detach().cpu(), np.float64).reshape(self.n_cells, 6)
+        elif activation is not None:
+            raise ValueError("activation is a muscle parameter")
+        key = (np.asarray(torch.as_tensor(mu).detach().cpu(), np.float64).tobytes(),
+               None if lam is None else np.asarray(torch.as_tensor(lam).detach().cpu(), np.float64).tobytes())
+        if act is not None and self._state is not None and self._key == key:
+            pot, sv, _, model = self._state
+            pot.set_activation(act)
+            opt = self._opt
+            fwd = Forward(model, opt)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            sol = fwd.step()
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            self._state = (pot, sv, fwd.state.u, model)
+            self.stats = AdjointStats(sol)
+            self.timings = {"build": t1 - t0, "forward": t2 - t1}
+            return fwd.state.u
         mesh = meshgen.TetMesh(self.points, self.cells)
         mesh.cell_data[MU] = np.asarray(torch.as_tensor(mu).detach().cpu(), np.float64)
         if lam is not None:
             mesh.cell_data[LAMBDA] = np.asarray(torch.as_tensor(lam).detach().cpu(), np.float64)
+        if act is not None:
+            mesh.cell_data["activation"] = act
         mesh.point_data[FIXED_MASK] = self.fixed_mask
         mesh.point_data[FIXED_VALUE] = self.fixed_values
         pot = self.material.from_pyvista(mesh, dtype=self.dtype)
@@ -100,12 +136,15 @@ class MaterialEquilibrium:
         t2 = time.perf_counter()
         u = fwd.state.u
         self._state = (pot, opt.solver(fwd.problem), u, model)
+        self._opt = opt
+        self._key = key
         self.stats = AdjointStats(sol)
         self.timings = {"build": t1 - t0, "forward": t2 - t1}
         return u
 
     def vjp(self, grad_u: torch.Tensor) -> dict:
-        """dL/dmu (and dL/dlambda) per cell for dL/du = grad_u at the last forward's u*."""
+        """dL/dmu (and dL/dlambda; dL/dactivation for the muscle) per cell for
+        dL/du = grad_u at the last forward's u*."""
         if self._state is None:
             raise RuntimeError("call solve() first")
         pot, sv, u, _ = self._state
@@ -123,15 +162,17 @@ class MaterialEquilibrium:
 
 
 class EquilibriumFunction(torch.autograd.Function):
-    """``u = EquilibriumFunction.apply(mu, lam, problem)``: the converged
-    displacement as a differentiable function of the per-cell materials
-    (``lam`` may be None for ARAP)."""
+    """``u = EquilibriumFunction.apply(mu, lam, problem[, activation])``: the
+    converged displacement as a differentiable function of the per-cell
+    materials (``lam`` may be None for ARAP; ``activation`` (n_cells, 6) for
+    the muscle)."""
 
     @staticmethod
-    def forward(ctx, mu, lam, problem: MaterialEquilibrium):
-        u = problem.solve(mu, lam)
+    def forward(ctx, mu, lam, problem: MaterialEquilibrium, activation=None):
+        u = problem.solve(mu, lam, activation)
         ctx.problem = problem
         ctx.has_lam = lam is not None
+        ctx.has_act = activation is not None
         ctx.mu_dtype = mu.dtype
         ctx.mu_device = mu.device
         return u.to(mu.dtype)
@@ -139,8 +180,8 @@ class EquilibriumFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_u):
         g = ctx.problem.vjp(grad_u)
-        dmu = g["mu"].to(dtype=ctx.mu_dtype, device=ctx.mu_device)
-        dlam = None
-        if ctx.has_lam and "lambda" in g:
-            dlam = g["lambda"].to(dtype=ctx.mu_dtype, device=ctx.mu_device)
-        return dmu, dlam, None
+        cast = lambda t: t.to(dtype=ctx.mu_dtype, device=ctx.mu_device)  # noqa: E731
+        dmu = cast(g["mu"])
+        dlam = cast(g["lambda"]) if ctx.has_lam and "lambda" in g else None
+        dact = cast(g["activation"]) if ctx.has_act and "activation" in g else None
+        return dmu, dlam, None, dact

@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kCgThreads) cg_prod_kernel(CgArgs c) {
   if (g < ge) {
     const int e0 = a.fv.group_estart[g];
     n = a.fv.group_estart[g + 1] - e0;
-    if (lane < n) load_elem<R>(a.fv, e0 + lane, geo, ids);
+    if (lane < n) load_elem_m<R, MAT>(a.fv, e0 + lane, geo, ids);
   }
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   pdl_trigger_cg();
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kCgThreads) cg_prod_kernel(CgArgs c) {
     if (gn < ge) {
       const int e0n = a.fv.group_estart[gn];
       nn = a.fv.group_estart[gn + 1] - e0n;
-      if (lane < nn) load_elem<R>(a.fv, e0n + lane, geon, idsn);
+      if (lane < nn) load_elem_m<R, MAT>(a.fv, e0n + lane, geon, idsn);
     }
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R f[4][3];
@@ -213,7 +213,8 @@ __global__ void __launch_bounds__(kCgThreads) cg_prod_kernel(CgArgs c) {
           for (int j = 0; j < 3; ++j)
             dF[i][j] = e[i][0] * geo.D[0][j] + e[i][1] * geo.D[1][j] + e[i][2] * geo.D[2][j];
       }
-      if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      add_act<MAT>(geo, G);
+      if constexpr (snh_family(MAT)) {
         SnhPoint<R> s;
         snh_prepare(G, s);
         SnhDir<R> d;
@@ -404,6 +405,7 @@ cudaError_t cg_prepare_t() {
   const cudaFuncAttribute m = cudaFuncAttributeMaxDynamicSharedMemorySize;
   cudaError_t e = cudaFuncSetAttribute(cg_prod_kernel<R, AGB_ARAP>, m, b);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(cg_prod_kernel<R, AGB_STABLE_NEO_HOOKEAN>, m, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(cg_prod_kernel<R, AGB_STABLE_NEO_HOOKEAN_MUSCLE>, m, b);
   return e;
 }
 
@@ -429,7 +431,7 @@ __global__ void __launch_bounds__(kElemThreads) param_vjp_kernel(FemView fv, con
   for (int e = fv.tile_estart[tile] + threadIdx.x; e < fv.tile_estart[tile + 1]; e += blockDim.x) {
     ElemGeo<R> geo;
     uint32_t ids;
-    load_elem<R>(fv, e, geo, ids);
+    load_elem_m<R, MAT>(fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R cu[4][3], cw[4][3], G[3][3], W[3][3];
 #pragma unroll
@@ -443,9 +445,10 @@ __global__ void __launch_bounds__(kElemThreads) param_vjp_kernel(FemView fv, con
       cw[k][2] = b.z;
     }
     corner_gradient(cu, geo.D, G);
-    corner_gradient(cw, geo.D, W);
+    add_act<MAT>(geo, G);
+    corner_gradient(cw, geo.D, W);  // muscle: W A (the records hold D A)
     R dmu, dlam = R(0);
-    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+    if constexpr (snh_family(MAT)) {
       // P = mu' (F - cof F) + lambda' (J - 1) cof F  (mu' = mu dV, lambda' = lambda dV)
       SnhPoint<R> s;
       snh_prepare(G, s);
@@ -466,6 +469,83 @@ __global__ void __launch_bounds__(kElemThreads) param_vjp_kernel(FemView fv, con
     const int c = elem_user[e];
     out_mu[c] += dv * dmu;
     if (out_lam) out_lam[c] += dv * dlam;
+  }
+}
+
+// d(w . grad)/d a for the muscle activation a (six entries per cell, A = I + sym(a)).
+// With F_m = F A = I + G_m, W' = sum_a w_a (D A)_a and P, dP premultiplied by dV:
+//   d/dA [P(F A) : W_0 A] = A^-1 (F_m^T dP[W'] + W'^T P(F_m))   (A symmetric)
+// and d/da = (Z00, Z11, Z22, Z01 + Z10, Z02 + Z20, Z12 + Z21)
+// (warp/fem/_stable_neo_hookean_muscle.py:18-46, func/_misc.py:48-53).
+template <class R>
+__global__ void __launch_bounds__(kElemThreads) activation_vjp_kernel(FemView fv, const V4<R>* __restrict__ u,
+                                                                      const V4<R>* __restrict__ w,
+                                                                      const int32_t* __restrict__ elem_user,
+                                                                      R* __restrict__ out_act) {
+  __shared__ V4<R> su[kTileVerts];
+  __shared__ V4<R> sw[kTileVerts];
+  const int tile = blockIdx.x;
+  const int vs = fv.tile_vstart[tile], nv = fv.tile_vstart[tile + 1] - vs;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    const int v = fv.tv_vid[vs + i];
+    su[i] = ldg4(u + v);
+    sw[i] = ldg4(w + v);
+  }
+  __syncthreads();
+  for (int e = fv.tile_estart[tile] + threadIdx.x; e < fv.tile_estart[tile + 1]; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem_m<R, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R cu[4][3], cw[4][3], G[3][3], W[3][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const V4<R> a = su[l[k]], b = sw[l[k]];
+      cu[k][0] = a.x;
+      cu[k][1] = a.y;
+      cu[k][2] = a.z;
+      cw[k][0] = b.x;
+      cw[k][1] = b.y;
+      cw[k][2] = b.z;
+    }
+    corner_gradient(cu, geo.D, G);
+    add_act<AGB_STABLE_NEO_HOOKEAN_MUSCLE>(geo, G);
+    corner_gradient(cw, geo.D, W);
+    SnhPoint<R> s;
+    snh_prepare(G, s);
+    R P[3][3], H[3][3];
+    snh_pk1(s, geo.mu, geo.lam, P);
+    SnhDir<R> d;
+    snh_dir(s, W, d);
+    snh_hess_prod(s, d, W, geo.mu, geo.lam, H);
+    R T[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        R t = R(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) t += (G[k][i] + (k == i ? R(1) : R(0))) * H[k][j] + W[k][i] * P[k][j];
+        T[i][j] = t;
+      }
+    R A[3][3] = {{R(1) + geo.S[0], geo.S[3], geo.S[4]},
+                 {geo.S[3], R(1) + geo.S[1], geo.S[5]},
+                 {geo.S[4], geo.S[5], R(1) + geo.S[2]}};
+    R cA[3][3];
+    cof3(A, cA);  // symmetric A: A^-1 = cof(A) / det(A)
+    const R inv_det = R(1) / det3(A);
+    R Z[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Z[i][j] = inv_det * (cA[i][0] * T[0][j] + cA[i][1] * T[1][j] + cA[i][2] * T[2][j]);
+    R* o = out_act + 6 * (size_t)elem_user[e];
+    o[0] += Z[0][0];
+    o[1] += Z[1][1];
+    o[2] += Z[2][2];
+    o[3] += Z[0][1] + Z[1][0];
+    o[4] += Z[0][2] + Z[2][0];
+    o[5] += Z[1][2] + Z[2][1];
   }
 }
 
@@ -492,10 +572,14 @@ cudaError_t launch_cg_iteration(const CgArgs& c, cudaStream_t s) {
   cudaError_t e;
   if (c.a.precision == AGB_F64)
     e = c.a.fv.material == AGB_ARAP ? cg_iteration_t<double, AGB_ARAP>(c, s)
-                                    : cg_iteration_t<double, AGB_STABLE_NEO_HOOKEAN>(c, s);
+        : c.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
+            ? cg_iteration_t<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(c, s)
+            : cg_iteration_t<double, AGB_STABLE_NEO_HOOKEAN>(c, s);
   else
     e = c.a.fv.material == AGB_ARAP ? cg_iteration_t<float, AGB_ARAP>(c, s)
-                                    : cg_iteration_t<float, AGB_STABLE_NEO_HOOKEAN>(c, s);
+        : c.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
+            ? cg_iteration_t<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(c, s)
+            : cg_iteration_t<float, AGB_STABLE_NEO_HOOKEAN>(c, s);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
@@ -518,8 +602,13 @@ cudaError_t launch_param_vjp(const FemView& fv, int precision, const void* u, co
                              const int32_t* elem_user, void* out_mu, void* out_lam, cudaStream_t s) {
   if (fv.n_tiles == 0) return cudaSuccess;
   const dim3 g(fv.n_tiles), b(kElemThreads);
+  const bool muscle = fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
   if (precision == AGB_F64) {
-    if (fv.material == AGB_ARAP)
+    if (muscle)
+      param_vjp_kernel<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<g, b, 0, s>>>(
+          fv, (const V4<double>*)u, (const V4<double>*)w, (const double*)vol, elem_user, (double*)out_mu,
+          (double*)out_lam);
+    else if (fv.material == AGB_ARAP)
       param_vjp_kernel<double, AGB_ARAP><<<g, b, 0, s>>>(fv, (const V4<double>*)u, (const V4<double>*)w,
                                                           (const double*)vol, elem_user, (double*)out_mu,
                                                           (double*)out_lam);
@@ -528,7 +617,11 @@ cudaError_t launch_param_vjp(const FemView& fv, int precision, const void* u, co
           fv, (const V4<double>*)u, (const V4<double>*)w, (const double*)vol, elem_user, (double*)out_mu,
           (double*)out_lam);
   } else {
-    if (fv.material == AGB_ARAP)
+    if (muscle)
+      param_vjp_kernel<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<g, b, 0, s>>>(
+          fv, (const V4<float>*)u, (const V4<float>*)w, (const float*)vol, elem_user, (float*)out_mu,
+          (float*)out_lam);
+    else if (fv.material == AGB_ARAP)
       param_vjp_kernel<float, AGB_ARAP><<<g, b, 0, s>>>(fv, (const V4<float>*)u, (const V4<float>*)w,
                                                          (const float*)vol, elem_user, (float*)out_mu,
                                                          (float*)out_lam);
@@ -537,6 +630,20 @@ cudaError_t launch_param_vjp(const FemView& fv, int precision, const void* u, co
           fv, (const V4<float>*)u, (const V4<float>*)w, (const float*)vol, elem_user, (float*)out_mu,
           (float*)out_lam);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_activation_vjp(const FemView& fv, int precision, const void* u, const void* w,
+                                  const int32_t* elem_user, void* out_act, cudaStream_t s) {
+  if (fv.n_tiles == 0) return cudaSuccess;
+  if (fv.material != AGB_STABLE_NEO_HOOKEAN_MUSCLE || !fv.act) return cudaErrorInvalidValue;
+  const dim3 g(fv.n_tiles), b(kElemThreads);
+  if (precision == AGB_F64)
+    activation_vjp_kernel<double><<<g, b, 0, s>>>(fv, (const V4<double>*)u, (const V4<double>*)w, elem_user,
+                                                  (double*)out_act);
+  else
+    activation_vjp_kernel<float><<<g, b, 0, s>>>(fv, (const V4<float>*)u, (const V4<float>*)w, elem_user,
+                                                 (float*)out_act);
   return cudaGetLastError();
 }
 

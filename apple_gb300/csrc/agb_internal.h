@@ -109,6 +109,11 @@ struct FemView {
   // FP32: rec = float4[3][n_cells]; FP64: rec = double[11][n_cells] + ids
   const void* rec;
   const uint32_t* ids;
+  // stable Neo-Hookean muscle: the activation offset S = A - I per element
+  // (A = I + sym(a), a the cell's 6-vector); FP32: float4[2][n_cells] =
+  // (S00 S11 S22 S01), (S02 S12 0 0); FP64: double[6][n_cells].  The records
+  // of a muscle potential hold D A instead of D.
+  const void* act;
 };
 }  // namespace agb
 
@@ -130,6 +135,8 @@ struct agb_fem {
   void* d_rec = nullptr;
   uint32_t* d_ids = nullptr;
   std::vector<double> vol_internal;  // dV * fraction per internal element
+  std::vector<double> act_internal;  // muscle: activation (6 per internal element)
+  void* d_act = nullptr;             // muscle: S stream (FemView::act)
   int32_t* d_elem_user = nullptr;    // internal -> caller's cell index (on first use)
   void* d_vol = nullptr;             // R per internal element (on first use)
   // scratch for the standalone evaluation API

@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kGradThreads) batch_ref_elem_kernel(BatchArgs 
   pdl_trigger();
   pdl_wait();
   if (!b.st[b.tile_mesh[blockIdx.x]].refresh) return;
-  ref_tile(b.a, blockIdx.x);
+  ref_tile<AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kVThreads) batch_ref_vertex_kernel(BatchArgs b) {

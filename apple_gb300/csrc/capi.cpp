@@ -56,32 +56,77 @@ void dfree(void* p) {
   } while (0)
 
 // element records of a plan in the kernels' layout
-int upload_records(const TilePlan& plan, int precision, void** d_rec, uint32_t** d_ids) {
+// D A per element (component-major like TilePlan::D) for activations
+// act[6 e + k] = (a00 a11 a22 a01 a02 a12); A = I + sym(a)
+std::vector<double> muscle_D(const TilePlan& plan, const std::vector<double>& act) {
   const size_t n = (size_t)plan.n_cells;
-  *d_ids = nullptr;
+  std::vector<double> out(9 * n);
+  for (size_t e = 0; e < n; ++e) {
+    const double* a = &act[6 * e];
+    const double A[3][3] = {{1.0 + a[0], a[3], a[4]}, {a[3], 1.0 + a[1], a[5]}, {a[4], a[5], 1.0 + a[2]}};
+    for (int r = 0; r < 3; ++r)
+      for (int j = 0; j < 3; ++j) {
+        double v = 0.0;
+        for (int m = 0; m < 3; ++m) v += plan.D[(3 * r + m) * n + e] * A[m][j];
+        out[(3 * r + j) * n + e] = v;
+      }
+  }
+  return out;
+}
+
+// the activation offset stream (FemView::act) of a muscle potential
+int upload_act(const std::vector<double>& act, size_t n, int precision, void** d_act) {
+  if (precision == AGB_F32) {
+    std::vector<float> v(8 * n, 0.0f);
+    for (size_t e = 0; e < n; ++e) {
+      const double* a = &act[6 * e];
+      float* s0 = &v[4 * e];
+      float* s1 = &v[4 * (n + e)];
+      s0[0] = (float)a[0];
+      s0[1] = (float)a[1];
+      s0[2] = (float)a[2];
+      s0[3] = (float)a[3];
+      s1[0] = (float)a[4];
+      s1[1] = (float)a[5];
+    }
+    if (!*d_act) RC(dalloc_bytes(d_act, v.size() * sizeof(float)));
+    return upload(*d_act, v.data(), v.size() * sizeof(float));
+  }
+  std::vector<double> v(6 * n);
+  for (size_t e = 0; e < n; ++e)
+    for (int k = 0; k < 6; ++k) v[k * n + e] = act[6 * e + k];
+  if (!*d_act) RC(dalloc_bytes(d_act, v.size() * sizeof(double)));
+  return upload(*d_act, v.data(), v.size() * sizeof(double));
+}
+
+int upload_records(const TilePlan& plan, int precision, void** d_rec, uint32_t** d_ids,
+                   const std::vector<double>* D_override = nullptr) {
+  const size_t n = (size_t)plan.n_cells;
+  const std::vector<double>& D = D_override ? *D_override : plan.D;
   if (precision == AGB_F32) {
     std::vector<float> rec(12 * n);
     for (size_t e = 0; e < n; ++e) {
       float* A = &rec[4 * e];
       float* B = &rec[4 * (n + e)];
       float* C = &rec[4 * (2 * n + e)];
-      for (int k = 0; k < 4; ++k) A[k] = (float)plan.D[k * n + e];
-      for (int k = 0; k < 4; ++k) B[k] = (float)plan.D[(4 + k) * n + e];
-      C[0] = (float)plan.D[8 * n + e];
+      for (int k = 0; k < 4; ++k) A[k] = (float)D[k * n + e];
+      for (int k = 0; k < 4; ++k) B[k] = (float)D[(4 + k) * n + e];
+      C[0] = (float)D[8 * n + e];
       C[1] = (float)plan.mudv[e];
       C[2] = (float)plan.lamdv[e];
       std::memcpy(&C[3], &plan.ids[e], 4);
     }
-    RC(dalloc_bytes(d_rec, rec.size() * sizeof(float)));
+    if (!*d_rec) RC(dalloc_bytes(d_rec, rec.size() * sizeof(float)));
     return upload(*d_rec, rec.data(), rec.size() * sizeof(float));
   }
   std::vector<double> rec(11 * n);
   for (size_t k = 0; k < 9; ++k)
-    std::memcpy(&rec[k * n], &plan.D[k * n], n * sizeof(double));
+    std::memcpy(&rec[k * n], &D[k * n], n * sizeof(double));
   std::memcpy(&rec[9 * n], plan.mudv.data(), n * sizeof(double));
   std::memcpy(&rec[10 * n], plan.lamdv.data(), n * sizeof(double));
-  RC(dalloc_bytes(d_rec, rec.size() * sizeof(double)));
+  if (!*d_rec) RC(dalloc_bytes(d_rec, rec.size() * sizeof(double)));
   RC(upload(*d_rec, rec.data(), rec.size() * sizeof(double)));
+  if (*d_ids) return upload(*d_ids, plan.ids.data(), plan.ids.size() * sizeof(uint32_t));
   return dupload(d_ids, plan.ids);
 }
 
@@ -106,6 +151,19 @@ std::vector<R> pack_v4(const std::vector<double>& xyz, const std::vector<uint8_t
   return out;
 }
 
+// internal -> caller cell index and dV * fraction on the device (first use)
+int ensure_vjp_tables(agb_fem* f) {
+  if (f->d_elem_user) return AGB_OK;
+  RC(dupload(&f->d_elem_user, f->plan.elem_user));
+  if (f->precision == AGB_F64) {
+    RC(dalloc_bytes(&f->d_vol, 8 * f->vol_internal.size()));
+    return upload(f->d_vol, f->vol_internal.data(), 8 * f->vol_internal.size());
+  }
+  std::vector<float> v(f->vol_internal.begin(), f->vol_internal.end());
+  RC(dalloc_bytes(&f->d_vol, 4 * v.size()));
+  return upload(f->d_vol, v.data(), 4 * v.size());
+}
+
 }  // namespace
 
 FemView agb_fem::view() const {
@@ -120,6 +178,7 @@ FemView agb_fem::view() const {
   v.tv_vid = d_tv_vid;
   v.rec = d_rec;
   v.ids = d_ids;
+  v.act = d_act;
   return v;
 }
 
@@ -202,7 +261,7 @@ int agb_fem_destroy(agb_fem* f) {
                   (void*)f->d_group_estart, (void*)f->d_tv_vid,
                   (void*)f->d_own_slot, (void*)f->d_own_off, f->d_rec, (void*)f->d_ids, f->d_u,
                   f->d_p, f->d_slots, (void*)f->d_partials, (void*)f->d_counter,
-                  (void*)f->d_elem_user, f->d_vol})
+                  (void*)f->d_elem_user, f->d_vol, f->d_act})
     dfree(p);
   delete f;
   return AGB_OK;
@@ -215,7 +274,8 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
   AGB_REQUIRE(out, AGB_E_INVALID, "agb_fem_create: out is null");
   *out = nullptr;
   AGB_REQUIRE(space, AGB_E_INVALID, "agb_fem_create: space is null");
-  AGB_REQUIRE(material == AGB_ARAP || material == AGB_STABLE_NEO_HOOKEAN, AGB_E_INVALID,
+  AGB_REQUIRE(material == AGB_ARAP || material == AGB_STABLE_NEO_HOOKEAN ||
+                  material == AGB_STABLE_NEO_HOOKEAN_MUSCLE, AGB_E_INVALID,
               "agb_fem_create: unknown material %d", material);
   AGB_REQUIRE(precision == AGB_F32 || precision == AGB_F64, AGB_E_INVALID,
               "agb_fem_create: unknown precision %d", precision);
@@ -257,7 +317,7 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
   std::vector<double> mudv(n_cells), lamdv(n_cells, 0.0);
   for (int e = 0; e < n_cells; ++e) {
     mudv[e] = mu[e] * vol[e];
-    if (lambda && material == AGB_STABLE_NEO_HOOKEAN) lamdv[e] = lambda[e] * vol[e];
+    if (lambda && material != AGB_ARAP) lamdv[e] = lambda[e] * vol[e];
   }
   std::vector<int32_t> cells_int(4 * (size_t)n_cells);
   for (size_t k = 0; k < cells_int.size(); ++k) cells_int[k] = space->internal_of_user[cells[k]];
@@ -296,6 +356,10 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
   if (!rc) rc = dupload(&f->d_own_slot, f->own_slots.slot_of_tv);
   if (!rc) rc = dupload(&f->d_own_off, f->own_off);
   if (!rc) rc = upload_records(P, precision, &f->d_rec, &f->d_ids);
+  if (!rc && material == AGB_STABLE_NEO_HOOKEAN_MUSCLE) {
+    f->act_internal.assign(6 * (size_t)n_cells, 0.0);
+    rc = upload_act(f->act_internal, (size_t)n_cells, precision, &f->d_act);
+  }
   if (!rc) rc = dalloc_bytes(&f->d_u, v4 * np);
   if (!rc) rc = dalloc_bytes(&f->d_p, v4 * np);
   if (!rc) rc = dalloc_bytes(&f->d_slots, v4 * 3 * (size_t)P.n_tv);
@@ -314,6 +378,37 @@ int agb_fem_info(const agb_fem* f, int32_t* n_tiles, int32_t* n_tv) {
   AGB_REQUIRE(f, AGB_E_INVALID, "agb_fem_info: null handle");
   if (n_tiles) *n_tiles = f->plan.n_tiles;
   if (n_tv) *n_tv = f->plan.n_tv;
+  return AGB_OK;
+}
+
+int agb_fem_cells(const agb_fem* f, int32_t* cells_out, uint32_t* tile_color_hash) {
+  AGB_REQUIRE(f && cells_out, AGB_E_INVALID, "agb_fem_cells: null argument");
+  const TilePlan& P = f->plan;
+  const std::vector<int32_t>& uoi = f->space->user_of_internal;
+  uint32_t h = 2166136261u;  // FNV-1a over (tile, group, element, corner order)
+  auto mix = [&h](uint32_t v) {
+    for (int k = 0; k < 4; ++k) {
+      h ^= (v >> (8 * k)) & 0xffu;
+      h *= 16777619u;
+    }
+  };
+  for (int t = 0; t < P.n_tiles; ++t) {
+    const int vs = P.tile_vstart[t];
+    for (int g = P.tile_gstart[t]; g < P.tile_gstart[t + 1]; ++g) {
+      mix((uint32_t)g);
+      for (int e = P.group_estart[g]; e < P.group_estart[g + 1]; ++e) {
+        const int eu = P.elem_user[e];
+        mix((uint32_t)eu);
+        for (int a = 0; a < 4; ++a) {
+          const int l = (int)((P.ids[e] >> (8 * a)) & 0xffu);
+          const int32_t v = uoi[P.tv_vid[vs + l]];
+          cells_out[4 * (size_t)eu + a] = v;
+          mix((uint32_t)v);
+        }
+      }
+    }
+  }
+  if (tile_color_hash) *tile_color_hash = h;
   return AGB_OK;
 }
 
@@ -550,6 +645,8 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   for (agb_fem* f : m->fems)
     AGB_REQUIRE(f->material == mat, AGB_E_INVALID,
                 "agb_solver_create: potentials of one solver must share a material");
+  AGB_REQUIRE(mat != AGB_STABLE_NEO_HOOKEAN_MUSCLE || m->fems.size() == 1, AGB_E_INVALID,
+              "agb_solver_create: a muscle model has one potential (its activation records are used in place)");
   agb_pncg_params prm;
   agb_pncg_default_params(&prm);
   if (params) prm = *params;
@@ -633,7 +730,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   if (!rc) rc = dalloc_bytes(&sv->d_gd, 2 * v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_p0, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_p1, v4 * np);
-  const bool delta = sv->precision == AGB_F32 && mat == AGB_STABLE_NEO_HOOKEAN && prm.refresh_ratio > 0.0;
+  const bool delta = sv->precision == AGB_F32 && mat != AGB_ARAP && prm.refresh_ratio > 0.0;
   if (!rc && delta) rc = dalloc_bytes(&sv->d_xref, v4 * np);
   if (!rc && delta) rc = dalloc_bytes(&sv->d_gref, v4 * np);
   if (!rc) rc = dalloc_bytes(&sv->d_slots, v4 * 2 * (size_t)m->n_slots);
@@ -975,17 +1072,7 @@ int agb_fem_grad_param_vjp(agb_fem* f, const void* u, const void* w, void* out_m
                            void* stream) {
   AGB_REQUIRE(f && u && w && out_mu, AGB_E_INVALID, "agb_fem_grad_param_vjp: null argument");
   cudaStream_t s = as_stream(stream);
-  if (!f->d_elem_user) {
-    RC(dupload(&f->d_elem_user, f->plan.elem_user));
-    if (f->precision == AGB_F64) {
-      RC(dalloc_bytes(&f->d_vol, 8 * f->vol_internal.size()));
-      RC(upload(f->d_vol, f->vol_internal.data(), 8 * f->vol_internal.size()));
-    } else {
-      std::vector<float> v(f->vol_internal.begin(), f->vol_internal.end());
-      RC(dalloc_bytes(&f->d_vol, 4 * v.size()));
-      RC(upload(f->d_vol, v.data(), 4 * v.size()));
-    }
-  }
+  RC(ensure_vjp_tables(f));
   const int np = f->space->n_points;
   RC(check_launch(launch_pack(f->precision, np, f->space->d_user_of_internal, u, f->d_u, w, f->d_p, s),
                   "pack"));
@@ -1318,6 +1405,32 @@ int agb_batch_read(agb_batch* b, void* u_out, agb_pncg_stats* stats, void* strea
   }
   for (int k = 0; k < n; ++k)
     AGB_REQUIRE(b->h_state[k].error == 0, AGB_E_DEVICE, "batch: device guard tripped in model %d", k);
+  return AGB_OK;
+}
+
+int agb_fem_set_activation(agb_fem* f, const double* activation) {
+  AGB_REQUIRE(f && activation, AGB_E_INVALID, "agb_fem_set_activation: null argument");
+  AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE, AGB_E_INVALID,
+              "agb_fem_set_activation: not a muscle potential");
+  const TilePlan& P = f->plan;
+  const size_t n = (size_t)P.n_cells;
+  for (size_t e = 0; e < n; ++e)
+    for (int k = 0; k < 6; ++k) f->act_internal[6 * e + k] = activation[6 * (size_t)P.elem_user[e] + k];
+  const std::vector<double> D = muscle_D(P, f->act_internal);
+  RC(upload_records(P, f->precision, &f->d_rec, &f->d_ids, &D));
+  return upload_act(f->act_internal, n, f->precision, &f->d_act);
+}
+
+int agb_fem_grad_activation_vjp(agb_fem* f, const void* u, const void* w, void* out_activation, void* stream) {
+  AGB_REQUIRE(f && u && w && out_activation, AGB_E_INVALID, "agb_fem_grad_activation_vjp: null argument");
+  AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE, AGB_E_INVALID,
+              "agb_fem_grad_activation_vjp: not a muscle potential");
+  cudaStream_t s = as_stream(stream);
+  RC(ensure_vjp_tables(f));
+  const int np = f->space->n_points;
+  RC(check_launch(launch_pack(f->precision, np, f->space->d_user_of_internal, u, f->d_u, w, f->d_p, s), "pack"));
+  RC(check_launch(launch_activation_vjp(f->view(), f->precision, f->d_u, f->d_p, f->d_elem_user, out_activation, s),
+                  "activation_vjp"));
   return AGB_OK;
 }
 

@@ -65,6 +65,7 @@ struct ElemGeo {
   R D[3][3];
   R mu;   // mu * dV
   R lam;  // lambda * dV
+  R S[6];  // muscle: A - I = sym(a) as (S00 S11 S22 S01 S02 S12); D holds D A
 };
 
 // Gradient of a corner field w (4 corners x 3): W = sum_a (w_a - w_0) D_a^T

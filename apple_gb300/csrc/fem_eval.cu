@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kElemThreads) fem_eval_kernel(
   for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
     ElemGeo<R> geo;
     uint32_t ids;
-    load_elem<R>(fv, e, geo, ids);
+    load_elem_m<R, MAT>(fv, e, geo, ids);
     int l[4];
     R uc[4][3];
 #pragma unroll
@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(kElemThreads) fem_eval_kernel(
     }
     R G[3][3];
     corner_gradient(uc, geo.D, G);
+    add_act<MAT>(geo, G);
     R dF[3][3];
     if (need_p) {
       R pc[4][3];
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(kElemThreads) fem_eval_kernel(
       corner_gradient(pc, geo.D, dF);
     }
     R f[4][3];
-    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+    if constexpr (snh_family(MAT)) {
       SnhPoint<R> s;
       snh_prepare(G, s);
       if (do_fun) sums[0].add(snh_energy(s, geo.mu, geo.lam));
@@ -250,11 +251,15 @@ cudaError_t launch_fem_eval(int precision, const FemView& fv, unsigned flags, co
   if (precision == AGB_F64) {
     if (fv.material == AGB_ARAP)
       AGB_EVAL_LAUNCH(double, AGB_ARAP);
+    else if (fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      AGB_EVAL_LAUNCH(double, AGB_STABLE_NEO_HOOKEAN_MUSCLE);
     else
       AGB_EVAL_LAUNCH(double, AGB_STABLE_NEO_HOOKEAN);
   } else {
     if (fv.material == AGB_ARAP)
       AGB_EVAL_LAUNCH(float, AGB_ARAP);
+    else if (fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      AGB_EVAL_LAUNCH(float, AGB_STABLE_NEO_HOOKEAN_MUSCLE);
     else
       AGB_EVAL_LAUNCH(float, AGB_STABLE_NEO_HOOKEAN);
   }

@@ -102,6 +102,8 @@ using namespace agb;
 extern "C" int agb_fem_fun_noalloc(agb_fem* fem, const void* u, double* output, void* stream) {
   AGB_REQUIRE(fem && u && output, AGB_E_INVALID, "agb_fem_fun_noalloc: null argument");
   const FemView fv = fem->view();
+  AGB_REQUIRE(fv.material != AGB_STABLE_NEO_HOOKEAN_MUSCLE, AGB_E_INVALID,
+              "agb_fem_fun_noalloc: muscle potentials are not supported; use agb_fem_fun");
   AGB_REQUIRE(fv.n_tiles <= kNoAllocMaxTiles, AGB_E_INVALID,
               "agb_fem_fun_noalloc: the mesh has %d tiles; this entry point holds partial sums for at "
               "most %d (use agb_fem_fun)",

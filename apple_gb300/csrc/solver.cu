@@ -52,10 +52,10 @@ static int dir_blocks(int n_tiles) { return n_tiles < kSMs * kDirCtasPerSM ? n_t
 
 template <class R, int MAT>
 __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel(SolveArgs a, int use_cond) {
-  constexpr int N = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 6 : 1;
+  constexpr int N = snh_family(MAT) ? 6 : 1;
   // float-float warp trees only for c2 (terms of both signs); p^T H p is a
   // sum of clamped non-negative terms, c3..c6 are higher-order corrections
-  constexpr unsigned FF = (MAT == AGB_STABLE_NEO_HOOKEAN) ? 0x2u : 0x0u;
+  constexpr unsigned FF = snh_family(MAT) ? 0x2u : 0x0u;
   __shared__ V4<R> sx[kTileVerts];
   __shared__ V4<R> sp[kTileVerts];
   __shared__ Acc<R> red[kWarps * N];
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   int e = es + threadIdx.x;
   ElemGeo<R> geo;
   uint32_t ids = 0;
-  if (e < ee) load_elem<R>(a.fv, e, geo, ids);
+  if (e < ee) load_elem_m<R, MAT>(a.fv, e, geo, ids);
   int vid = tile_vertex(a.fv, tile, threadIdx.x);
   if (st->done) return;
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
@@ -100,12 +100,13 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
       if (last) en = esn + threadIdx.x;
       ElemGeo<R> geon;
       uint32_t idsn = 0;
-      if (last ? en < een : true) load_elem<R>(a.fv, en, geon, idsn);
+      if (last ? en < een : true) load_elem_m<R, MAT>(a.fv, en, geon, idsn);
       const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
       R G[3][3], dF[3][3];
       vec_gradient(sx, l, geo.D, G);
+      add_act<MAT>(geo, G);
       vec_gradient(sp, l, geo.D, dF);
-      if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      if constexpr (snh_family(MAT)) {
         SnhPoint<R> s;
         snh_prepare(G, s);
         SnhDir<R> d;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
     }
     if (!had) {  // no element of this tile for this thread: start on the next tile
       e = esn + threadIdx.x;
-      if (e < een) load_elem<R>(a.fv, e, geo, ids);
+      if (e < een) load_elem_m<R, MAT>(a.fv, e, geo, ids);
     }
     es = esn;
     ee = een;
@@ -225,7 +226,7 @@ size_t solver_grad_smem(int precision) {
 }
 
 template <class R, int MAT, bool DELTA>
-__global__ void __launch_bounds__(kGradThreads, MAT == AGB_STABLE_NEO_HOOKEAN ? 7 : 5) solver_grad_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(kGradThreads, snh_family(MAT) ? 7 : 5) solver_grad_kernel(SolveArgs a) {
   grad_tile<R, MAT, DELTA>(a, blockIdx.x, a.st);
 }
 
@@ -296,11 +297,12 @@ __global__ void __launch_bounds__(256) solver_energy_kernel(SolveArgs a) {
 // refresh of the reference state (FP32 stable Neo-Hookean); in the iteration
 // graph both follow the vertex pass as programmatic dependents and return at
 // once unless it asked for a refresh
+template <int MAT>
 __global__ void __launch_bounds__(kGradThreads) solver_ref_elem_kernel(SolveArgs a) {
   pdl_trigger();
   pdl_wait();
   if (!a.st->refresh) return;
-  ref_tile(a, blockIdx.x);
+  ref_tile<MAT>(a, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kVThreads) solver_ref_vertex_kernel(SolveArgs a) {
@@ -392,6 +394,9 @@ static cudaError_t prepare_t() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN, false>, m, g);
   if (e == cudaSuccess && kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>)
     e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>, m, g);
+  constexpr int MU = AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, MU, false>, m, g);
+  if (e == cudaSuccess && kRefDelta<R, MU>) e = cudaFuncSetAttribute(solver_grad_kernel<R, MU, kRefDelta<R, MU>>, m, g);
   return e;
 }
 
@@ -422,12 +427,16 @@ cudaError_t launch_solver_energy(const SolveArgs& a, cudaStream_t s) {
   if (a.precision == AGB_F64) {
     if (a.fv.material == AGB_ARAP)
       solver_energy_pass_kernel<double, AGB_ARAP><<<nt, kElemThreads, 0, s>>>(a);
+    else if (a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      solver_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<nt, kElemThreads, 0, s>>>(a);
     else
       solver_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN><<<nt, kElemThreads, 0, s>>>(a);
     solver_energy_kernel<double><<<1, 256, 0, s>>>(a);
   } else {
     if (a.fv.material == AGB_ARAP)
       solver_energy_pass_kernel<float, AGB_ARAP><<<nt, kElemThreads, 0, s>>>(a);
+    else if (a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      solver_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<nt, kElemThreads, 0, s>>>(a);
     else
       solver_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN><<<nt, kElemThreads, 0, s>>>(a);
     solver_energy_kernel<float><<<1, 256, 0, s>>>(a);
@@ -486,11 +495,15 @@ static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool firs
   if (a.precision == AGB_F64) {
     if (a.fv.material == AGB_ARAP)
       e = launch_iteration_t<double, AGB_ARAP>(a, use_cond, first, max_bt, s);
+    else if (a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      e = launch_iteration_t<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(a, use_cond, first, max_bt, s);
     else
       e = launch_iteration_t<double, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
   } else {
     if (a.fv.material == AGB_ARAP)
       e = launch_iteration_t<float, AGB_ARAP>(a, use_cond, first, max_bt, s);
+    else if (a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      e = launch_iteration_t<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(a, use_cond, first, max_bt, s);
     else
       e = launch_iteration_t<float, AGB_STABLE_NEO_HOOKEAN>(a, use_cond, first, max_bt, s);
   }
@@ -518,9 +531,13 @@ static cudaError_t launch_pass_t(const SolveArgs& a, int which, cudaStream_t s) 
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s) {
   if (a.precision == AGB_F64) {
     if (a.fv.material == AGB_ARAP) return launch_pass_t<double, AGB_ARAP>(a, which, s);
+    if (a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+      return launch_pass_t<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(a, which, s);
     return launch_pass_t<double, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
   }
   if (a.fv.material == AGB_ARAP) return launch_pass_t<float, AGB_ARAP>(a, which, s);
+  if (a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE)
+    return launch_pass_t<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(a, which, s);
   return launch_pass_t<float, AGB_STABLE_NEO_HOOKEAN>(a, which, s);
 }
 
@@ -546,9 +563,12 @@ cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_
 
 cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s) {
   if (!a.delta) return cudaSuccess;
-  if (!a.xref || !a.gref || a.precision != AGB_F32 || a.fv.material != AGB_STABLE_NEO_HOOKEAN)
-    return cudaErrorInvalidValue;
-  cudaError_t e = launch_pdl(solver_ref_elem_kernel, dim3(a.fv.n_tiles), dim3(kGradThreads), ref_smem_bytes(), s, a);
+  if (!a.xref || !a.gref || a.precision != AGB_F32 || !snh_family(a.fv.material)) return cudaErrorInvalidValue;
+  cudaError_t e = a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
+                      ? launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN_MUSCLE>, dim3(a.fv.n_tiles),
+                                   dim3(kGradThreads), ref_smem_bytes(), s, a)
+                      : launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN>, dim3(a.fv.n_tiles),
+                                   dim3(kGradThreads), ref_smem_bytes(), s, a);
   if (e == cudaSuccess) e = launch_pdl(solver_ref_vertex_kernel, dim3(a.vblocks), dim3(kVThreads), 0, s, a);
   return e != cudaSuccess ? e : cudaGetLastError();
 }

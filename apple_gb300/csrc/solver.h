@@ -191,6 +191,9 @@ cudaError_t launch_cg_iteration(const CgArgs& c, cudaStream_t s);
 cudaError_t launch_cg_set_limit(const CgArgs& c, int n, cudaStream_t s);
 cudaError_t launch_cg_unpack(const CgArgs& c, const int32_t* user_of_internal, void* out_user,
                              cudaStream_t s);
+// muscle: out_act[6 c + k] += d(w . grad)/d a_{c,k}, cells in the caller's order
+cudaError_t launch_activation_vjp(const FemView& fv, int precision, const void* u_int, const void* w_int,
+                                  const int32_t* elem_user, void* out_act, cudaStream_t s);
 // out_mu[c] += d(w . grad)/d mu_c (and lambda), cells in the caller's order
 cudaError_t launch_param_vjp(const FemView& fv, int precision, const void* u_int, const void* w_int,
                              const void* vol, const int32_t* elem_user, void* out_mu, void* out_lam,

@@ -198,7 +198,7 @@ __device__ __forceinline__ void dir_decide(SolverState* st, const double* tot) {
   const double gd = st->gd;
   const double a0 = initial_alpha(gd, hq, st->overstep);
   st->alpha0 = a0;
-  if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+  if constexpr (snh_family(MAT)) {
     double t = a0, de = 0.0;
     int ls = 0;
     bool ok = false;
@@ -360,7 +360,7 @@ __device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0,
 // Whether a solver instantiation uses the reference-state correction: FP32
 // stable Neo-Hookean (FP64 has the precision; ARAP is not polynomial).
 template <class R, int MAT>
-constexpr bool kRefDelta = MAT == AGB_STABLE_NEO_HOOKEAN && sizeof(R) == 4;
+constexpr bool kRefDelta = snh_family(MAT) && sizeof(R) == 4;
 
 // x + t p relative to the reference: (x_ref, d.x) and (d.y, d.z) per vertex,
 // d = (x_hi + t p - x_ref) + x_lo with the hi/lo pair updated by two-sum
@@ -434,7 +434,7 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
   if (g < ge) {
     const int e0 = a.fv.group_estart[g];
     n = a.fv.group_estart[g + 1] - e0;
-    if (lane < n) load_elem<R>(a.fv, e0 + lane, geo, ids);
+    if (lane < n) load_elem_m<R, MAT>(a.fv, e0 + lane, geo, ids);
   }
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   int vid[kGradVerts], sidx[kGradVerts];
@@ -468,7 +468,7 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
     if (gn < ge) {
       const int e0n = a.fv.group_estart[gn];
       nn = a.fv.group_estart[gn + 1] - e0n;
-      if (lane < nn) load_elem<R>(a.fv, e0n + lane, geon, idsn);
+      if (lane < nn) load_elem_m<R, MAT>(a.fv, e0n + lane, geon, idsn);
     }
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R f[4][3], hd[4][3];
@@ -478,13 +478,15 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
         // f_e(x) - f_e(x_ref) from P(A + dG) - P(A); energy and diagonal at A + dG
         R dG[3][3];
         delta_gradient(sh, sl, l, geo.D, G, dG);
+        add_act<MAT>(geo, G);
         SnhPoint<R> s, s2;
         snh_prepare(G, s);
         snh_pk1_delta(s, dG, geo.mu, geo.lam, P, s2);
         corner_vjp(P, geo.D, f);
         snh_hess_diag(s2, geo.D, geo.mu, geo.lam, hd);
-      } else if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+      } else if constexpr (snh_family(MAT)) {
         pair_gradient(sh, sl, l, geo.D, G);
+        add_act<MAT>(geo, G);
         SnhPoint<R> s;
         snh_prepare(G, s);
         snh_pk1(s, geo.mu, geo.lam, P);
@@ -560,6 +562,7 @@ __host__ __device__ constexpr size_t ref_smem_bytes() {
   return (size_t)kTileVerts * (size_t)(kGradWarps + 1) * sizeof(V4<double>);
 }
 
+template <int MAT>
 __device__ __forceinline__ void ref_tile(const SolveArgs& a, int tile) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V4<double>* sx = reinterpret_cast<V4<double>*>(smem_raw);
@@ -584,7 +587,7 @@ __device__ __forceinline__ void ref_tile(const SolveArgs& a, int tile) {
     if (lane < n) {
       ElemGeo<float> gf;
       uint32_t ids;
-      load_elem<float>(a.fv, e0 + lane, gf, ids);
+      load_elem_m<float, MAT>(a.fv, e0 + lane, gf, ids);
       ElemGeo<double> geo;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -593,9 +596,12 @@ __device__ __forceinline__ void ref_tile(const SolveArgs& a, int tile) {
       geo.mu = (double)gf.mu;
       geo.lam = (double)gf.lam;
 #pragma unroll
+      for (int k = 0; k < 6; ++k) geo.S[k] = (double)gf.S[k];
+#pragma unroll
       for (int k = 0; k < 4; ++k) l[k] = corner(ids, k);
       double G[3][3], P[3][3];
       vec_gradient(sx, l, geo.D, G);
+      add_act<MAT>(geo, G);
       SnhPoint<double> s;
       snh_prepare(G, s);
       snh_pk1(s, geo.mu, geo.lam, P);
@@ -678,11 +684,12 @@ __device__ __forceinline__ void energy_tile(const SolveArgs& a, int tile, AccSto
   for (int e = a.fv.tile_estart[tile] + threadIdx.x; e < a.fv.tile_estart[tile + 1]; e += blockDim.x) {
     ElemGeo<R> geo;
     uint32_t ids;
-    load_elem<R>(a.fv, e, geo, ids);
+    load_elem_m<R, MAT>(a.fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R G[3][3];
     pair_gradient(sh, sl, l, geo.D, G);
-    if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN) {
+    add_act<MAT>(geo, G);
+    if constexpr (snh_family(MAT)) {
       SnhPoint<R> s;
       snh_prepare(G, s);
       sums[0].add(snh_energy(s, geo.mu, geo.lam));

@@ -72,6 +72,55 @@ __device__ __forceinline__ void load_elem<double>(const FemView& fv, int e, Elem
   ids = __ldg(fv.ids + e);
 }
 
+// the stable Neo-Hookean family (plain and muscle) shares the element math
+constexpr bool snh_family(int mat) { return mat != AGB_ARAP; }
+
+// Muscle (warp/fem/_stable_neo_hookean_muscle.py:18-114): G_m = F A with
+// A = I + sym(a).  The records hold D A, so grad(u) A = sum_a (u_a - u_0) (D A)_a
+// comes out of the usual corner gradient, and G_m - I = S + grad(u) A with
+// S = A - I from the activation stream.
+template <class R>
+__device__ __forceinline__ void load_act(const FemView& fv, int e, ElemGeo<R>& g);
+template <>
+__device__ __forceinline__ void load_act<float>(const FemView& fv, int e, ElemGeo<float>& g) {
+  const float4* a = static_cast<const float4*>(fv.act);
+  const float4 s0 = __ldg(a + e), s1 = __ldg(a + (size_t)fv.n_cells + e);
+  g.S[0] = s0.x;
+  g.S[1] = s0.y;
+  g.S[2] = s0.z;
+  g.S[3] = s0.w;
+  g.S[4] = s1.x;
+  g.S[5] = s1.y;
+}
+template <>
+__device__ __forceinline__ void load_act<double>(const FemView& fv, int e, ElemGeo<double>& g) {
+  const double* a = static_cast<const double*>(fv.act);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) g.S[k] = __ldg(a + (size_t)k * fv.n_cells + e);
+}
+
+template <class R, int MAT>
+__device__ __forceinline__ void load_elem_m(const FemView& fv, int e, ElemGeo<R>& g, uint32_t& ids) {
+  load_elem<R>(fv, e, g, ids);
+  if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN_MUSCLE) load_act<R>(fv, e, g);
+}
+
+// G += S for the muscle (no-op otherwise)
+template <int MAT, class R>
+__device__ __forceinline__ void add_act(const ElemGeo<R>& g, R (&G)[3][3]) {
+  if constexpr (MAT == AGB_STABLE_NEO_HOOKEAN_MUSCLE) {
+    G[0][0] += g.S[0];
+    G[1][1] += g.S[1];
+    G[2][2] += g.S[2];
+    G[0][1] += g.S[3];
+    G[1][0] += g.S[3];
+    G[0][2] += g.S[4];
+    G[2][0] += g.S[4];
+    G[1][2] += g.S[5];
+    G[2][1] += g.S[5];
+  }
+}
+
 // correctly rounded primitives, so that every kernel that forms the PNCG
 // direction or the trial point computes bit-identical values
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }

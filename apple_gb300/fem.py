@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .region import FRACTION, LAMBDA, MU, Region, cell_data
+from .region import ACTIVATION, FRACTION, LAMBDA, MU, Region, cell_data
 
 _counter: dict[str, int] = {}
 
@@ -181,6 +181,14 @@ class WarpPotentialFem:
         _lib.call("agb_fem_info", self._standalone(), ctypes.byref(nt), ctypes.byref(ntv))
         return nt.value, ntv.value
 
+    def stored_cells(self) -> tuple[np.ndarray, int]:
+        """(cells as stored after reorder / tiling / colouring, in the caller's
+        cell order and point ids; hash of the tile and colour plan)."""
+        out = np.empty((self.cells.shape[0], 4), np.int32)
+        h = ctypes.c_uint32()
+        _lib.call("agb_fem_cells", self._standalone(), out.ctypes.data, ctypes.byref(h))
+        return out, h.value
+
     def __del__(self):
         if _lib._lib is None:
             return
@@ -235,7 +243,7 @@ class WarpPotentialFem:
         _lib.call("agb_fem_grad_param_vjp", self._standalone(), ptr(u), ptr(w), ptr(dmu), ptr(dlam),
                   stream_ptr(u.device))
         out = {"mu": dmu}
-        if self.material == _lib.STABLE_NEO_HOOKEAN:
+        if self.material != _lib.ARAP:
             out["lambda"] = dlam
         return out
 
@@ -280,6 +288,61 @@ class StableNeoHookean(WarpPotentialFem):
     (warp/fem/_stable_neo_hookean.py:17-27); cell data ``mu`` and ``lambda``."""
 
     material = _lib.STABLE_NEO_HOOKEAN
+
+
+def _activation_array(activation, n_cells: int) -> np.ndarray:
+    """(n_cells, 6) float64 from None (zeros), one 6-vector, or per-cell rows."""
+    if activation is None:
+        return np.zeros((n_cells, 6))
+    a = np.asarray(activation, np.float64)
+    if a.shape == (6,):
+        a = np.broadcast_to(a, (n_cells, 6))
+    return np.ascontiguousarray(a.reshape(n_cells, 6)).copy()
+
+
+class StableNeoHookeanMuscle(WarpPotentialFem):
+    """Stable Neo-Hookean of G = F A with the per-cell activation
+    A = I + [[a0, a3, a4], [a3, a1, a5], [a4, a5, a2]]
+    (warp/fem/_stable_neo_hookean_muscle.py:18-46, func/_misc.py:48-53);
+    cell data ``mu``, ``lambda`` and ``activation`` (n_cells, 6)."""
+
+    material = _lib.STABLE_NEO_HOOKEAN_MUSCLE
+
+    def __init__(self, cells, mu, lam=None, *, activation=None, **kw):
+        super().__init__(cells, mu, lam, **kw)
+        n = self.cells.shape[0]
+        self.activation = _activation_array(activation, n)
+
+    @classmethod
+    def from_region(cls, region: Region, **kw):
+        cd = region.cell_data
+        key = "activation" if "activation" in cd else ACTIVATION
+        if "activation" not in kw:
+            kw["activation"] = np.asarray(cd[key], np.float64).reshape(-1, 6) if key in cd else None
+        return super().from_region(region, **kw)
+
+    def _create(self, space: Space) -> ctypes.c_void_p:
+        h = super()._create(space)
+        _lib.call("agb_fem_set_activation", h, self.activation.ctypes.data)
+        return h
+
+    def set_activation(self, activation) -> None:
+        """Replace the per-cell activation on every device copy of this potential
+        (solvers built on it see the new records at their next launch)."""
+        self.activation = _activation_array(activation, self.cells.shape[0])
+        handles = list(self._by_space.values()) + ([self._own[1]] if self._own is not None else [])
+        for h in handles:
+            _lib.call("agb_fem_set_activation", h, self.activation.ctypes.data)
+
+    def grad_param_vjp(self, u: torch.Tensor, w: torch.Tensor) -> dict:
+        """As :meth:`WarpPotentialFem.grad_param_vjp`, plus ``"activation"``:
+        d(w.grad(u))/d activation, (n_cells, 6)."""
+        out = super().grad_param_vjp(u, w)
+        w = check_vec(w.to(self.dtype), self.n_points, self.dtype, "w")
+        da = torch.zeros((self.cells.shape[0], 6), dtype=self.dtype, device=u.device)
+        _lib.call("agb_fem_grad_activation_vjp", self._standalone(), ptr(u), ptr(w), ptr(da), stream_ptr(u.device))
+        out["activation"] = da
+        return out
 
 
 def with_lame(mesh, mu, lam=None):

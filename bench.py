@@ -55,9 +55,11 @@ def _args():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
-    ap.add_argument("--config", choices=["plain", "adjoint", "batched"], default="plain",
+    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular"], default="plain",
                     help="plain: the headline PNCG line; adjoint: the 138k-tet adjoint workload; "
-                         "batched: 512 uneven meshes in one batch vs solved one by one")
+                         "batched: 512 uneven meshes in one batch vs solved one by one; grid64: the "
+                         "64x64x96 grid (ARAP and stable Neo-Hookean, FP32 and FP64); irregular: the "
+                         "Delaunay ball")
     ap.add_argument("--n-meshes", type=int, default=512, help="batched: number of meshes")
     ap.add_argument("--fd-cells", type=int, default=32, help="adjoint: cells checked by central differences")
     ap.add_argument("--profile", action="store_true",
@@ -290,6 +292,20 @@ def run_ours(a) -> None:
     if tp.exists():
         traffic = json.loads(tp.read_text()).get(names[k])
 
+    # the spec solve: PNCG from the initial state to ||g||/||g0|| <= 1e-6
+    solve_opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=20000, rtol=1e-6))
+    solve_sv = solve_opt.solver(ag.ForwardProblem(model))
+    solve_sv.reset(u0)
+    solve_sv.iterate(1)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    solve_sv.reset(u0)
+    solve_sv.iterate(20000)
+    ssol = solve_sv.read()
+    t_solve = time.perf_counter() - t0
+    solve = {"rtol": 1e-6, "result": ssol.result.name, "iters": ssol.n_steps, "seconds": t_solve,
+             "rel_grad": ssol.grad_norm / ssol.grad_norm_first, "iters_per_s": ssol.n_steps / t_solve}
+
     # end to end through the public host-buffer API
     e2e_opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=a.e2e_iters, rtol=0.0))
     e2e_solver = e2e_opt.solver(ag.ForwardProblem(model))
@@ -327,13 +343,15 @@ def run_ours(a) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD if not a.small else "snh_grid_16x16x40", "n_tets": nt,
                        "n_vertices": nv, "E": E_MOD, "nu": NU, "step": "one PNCG iteration (one CUDA graph)",
-                       "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}"},
+                       "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}",
+                       "fp32_reference_correction": "on, FP64 refresh each 100x drop of ||g|| (solver default)"},
             "hbm_gbs_algorithmic": b_iter * value / world / 1e9,
             "roofline": {"bound": "hbm", "kernel": names[k], "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "bytes_per_launch": per_launch[names[k]], "ms_per_launch": ms[k]},
             "passes_ms": {n: ms[i] for i, n in enumerate(names)},
             "e2e": e2e,
+            "solve_to_1e-6": solve,
             "cpu_baseline": cpu,
             "gpu_launches": 3 * a.steps,
             "clocks": clk,
@@ -559,6 +577,183 @@ def run_batched(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _timed_steps(sv, steps, warmup, dev):
+    import statistics
+
+    import torch
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for i in range(warmup):
+        flush.fill_(i & 0xFF)
+        sv.step()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize(dev)
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        sv.step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms = [x.elapsed_time(y) for x, y in ev]
+    return statistics.median(ms), sum(ms)
+
+
+def _solve_case(model, u0, rtol, max_steps, dev):
+    import apple_gb300 as ag
+    import torch
+
+    opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=max_steps, rtol=rtol))
+    sv = opt.solver(ag.ForwardProblem(model))
+    sv.reset(u0)
+    sv.iterate(1)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    sv.reset(u0)
+    sv.iterate(max_steps)
+    u = torch.empty_like(u0)
+    sol = sv.read(u)
+    return sol, time.perf_counter() - t0, u
+
+
+def run_grid64(a) -> None:
+    """The 64x64x96-cell grid (1,966,080 tets): iteration speed of ARAP (mu = 1) and
+    stable Neo-Hookean in FP32 and FP64, and the FP32 energy / gradient / solution
+    error against the FP64 oracle."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+    from oracle import fem_oracle as O
+
+    nx, ny, nz = (16, 16, 24) if a.small else (64, 64, 96)
+    m = meshgen.grid(nx, ny, nz, h=1.0 / nx)
+    lam, mu = meshgen.lame_converter(E_MOD, NU)
+    mask = np.zeros((m.n_points, 3), bool)
+    fv = np.zeros((m.n_points, 3))
+    mask[meshgen.face_mask(m, 2, "min")] = True
+    top = meshgen.face_mask(m, 2, "max")
+    mask[top] = True
+    fv[top, 2] = STRETCH * m.points[:, 2].max()
+    dev = torch.device("cuda")
+    out = {"metric": "PNCG iters/s on the 64x64x96 grid", "config": {
+        "workload": "grid_64x64x96_1.97M_tets_stretch30" if not a.small else "grid_16x16x24", "n_tets": m.n_cells,
+        "n_vertices": m.n_points, "E": E_MOD, "nu": NU, "arap_mu": 1.0}, "variants": {}}
+    B_iter = {"snh": 64 * m.n_cells + 84 * m.n_points, "arap": 60 * m.n_cells + 84 * m.n_points}
+    peak, _ = _measured_peak()
+    for mat in ("snh", "arap"):
+        for dtype in (torch.float32, torch.float64):
+            mesh = meshgen.TetMesh(m.points, m.cells)
+            if mat == "snh":
+                mesh = ag.with_lame(mesh, mu, lam)
+                cls = ag.StableNeoHookean
+            else:
+                mesh.cell_data["mu"] = np.ones(m.n_cells)
+                cls = ag.Arap
+            mesh.point_data["FixedMask"] = mask
+            mesh.point_data["FixedValue"] = fv
+            b = ag.ModelBuilder(dtype=dtype)
+            b.add_vertices(mesh)
+            b.add_fixed(mesh)
+            b.add_potential(cls.from_pyvista(mesh, dtype=dtype))
+            model = b.finalize()
+            u0 = torch.tensor(np.where(mask, fv, 0.0), dtype=dtype, device=dev)
+            opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=2**30, rtol=0.0))
+            sv = opt.solver(ag.ForwardProblem(model))
+            sv.reset(u0)
+            steps = 30 if dtype == torch.float64 else 300
+            med, tot = _timed_steps(sv, steps, 5, dev)
+            key = f"{mat}_{'f32' if dtype == torch.float32 else 'f64'}"
+            v = {"iters_per_s": steps / (tot / 1e3), "ms_per_iter_median": med,
+                 "hbm_gbs_algorithmic": B_iter[mat] * steps / (tot / 1e3) / 1e9}
+            v["frac_of_measured_hbm"] = v["hbm_gbs_algorithmic"] / peak
+            if dtype == torch.float32:
+                # FP32 vs FP64 oracle at the iterate reached after the timed steps
+                u = torch.empty_like(u0)
+                sv.read(u)
+                u64 = u.double().cpu().numpy()
+                ora = O.FemPotential.from_mesh(O.Material.STABLE_NEO_HOOKEAN if mat == "snh" else O.Material.ARAP,
+                                               m.points, m.cells, mu=mu if mat == "snh" else 1.0,
+                                               lam=lam if mat == "snh" else None)
+                pot = model.warp_model.potentials[next(iter(model.warp_model.potentials))]
+                ev = pot.eval(u, fun=True, grad=True)
+                e_ref = ora.fun(u64)
+                g_ref = ora.grad(u64)
+                v["energy_rel_err_vs_fp64_oracle"] = abs(ev["fun"].item() / e_ref - 1.0)
+                v["grad_rel_l2_err_vs_fp64_oracle"] = float(np.linalg.norm(ev["grad"].double().cpu().numpy() - g_ref)
+                                                            / np.linalg.norm(g_ref))
+            out["variants"][key] = v
+    print(json.dumps(out), flush=True)
+
+
+def run_irregular(a) -> None:
+    """The irregular workload: a seeded Delaunay ball (300k interior + 20k shell
+    points, random vertex order, per-tet mu log-uniform in [1e3, 1e6], lambda =
+    10 mu): PNCG iteration speed in FP32, and the bit-exact check that the
+    Morton reorder and the tile colouring keep every cell's four corners."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+
+    n_in, n_sh = (20000, 3000) if a.small else (300000, 20000)
+    t0 = time.perf_counter()
+    m = meshgen.ball(n_in, n_sh, seed=0)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(m.n_points)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(m.n_points)
+    pts = m.points[perm]
+    cells = inv[m.cells].astype(np.int32)
+    t_mesh = time.perf_counter() - t0
+    mu = np.exp(rng.uniform(np.log(1e3), np.log(1e6), cells.shape[0]))
+    mesh = meshgen.TetMesh(pts, cells)
+    mesh.cell_data["mu"] = mu
+    mesh.cell_data["lambda"] = 10.0 * mu
+    r = np.linalg.norm(pts, axis=1)
+    mask = np.zeros((pts.shape[0], 3), bool)
+    mask[pts[:, 2] < -0.9] = True  # a fixed cap
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = np.zeros((pts.shape[0], 3))
+    f = meshgen.lumped_gravity(mesh, 1000.0) * 100.0
+    b = ag.ModelBuilder()
+    b.add_vertices(mesh)
+    b.add_fixed(mesh)
+    pot = ag.StableNeoHookean.from_pyvista(mesh)
+    b.add_potential(pot)
+    fm = meshgen.TetMesh(pts, cells)
+    fm.point_data["Force"] = f
+    fm.point_data["GlobalPointId"] = np.arange(pts.shape[0])
+    b.add_potential(ag.ExternalForce.from_pyvista(fm))
+    model = b.finalize()
+    dev = torch.device("cuda")
+    u0 = torch.zeros((pts.shape[0], 3), dtype=torch.float32, device=dev)
+    opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=2**30, rtol=0.0))
+    sv = opt.solver(ag.ForwardProblem(model))
+    sv.reset(u0)
+    med, tot = _timed_steps(sv, 300, 5, dev)
+    # connectivity as stored after the Morton reorder and the colouring: every
+    # cell keeps its corner set; the plan is the same when built again
+    stored, h1 = pot.stored_cells()
+    _, h2 = ag.StableNeoHookean.from_pyvista(mesh).stored_cells()
+    exact = bool(np.array_equal(np.sort(stored, axis=1), np.sort(cells, axis=1)))
+    sol, t_solve, _ = _solve_case(model, u0, 1e-6, 5000, dev)
+    nt, ntv = pot.info()
+    line = {"metric": "PNCG iters/s on the irregular Delaunay ball",
+            "config": {"workload": "snh_delaunay_ball_320k_points" if not a.small else "snh_delaunay_ball_small",
+                       "n_tets": int(cells.shape[0]), "n_vertices": int(pts.shape[0]), "mu": "log-uniform [1e3, 1e6]",
+                       "lambda": "10 mu", "load": "100 g body force, cap z < -0.9 fixed"},
+            "iters_per_s": 300 / (tot / 1e3), "ms_per_iter_median": med,
+            "hbm_gbs_algorithmic": (64 * cells.shape[0] + 84 * pts.shape[0]) * 300 / (tot / 1e3) / 1e9,
+            "tiles": nt, "tile_vertices_per_vertex": ntv / pts.shape[0],
+            "connectivity_exact": exact, "plan_hash": h1, "plan_rebuild_identical": h1 == h2, "mesh_s": t_mesh,
+            "solve": {"rtol": 1e-6, "max_steps": 5000, "result": sol.result.name, "iters": sol.n_steps,
+                      "seconds": t_solve, "rel_grad": sol.grad_norm / sol.grad_norm_first}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
@@ -567,6 +762,10 @@ def main():
         run_adjoint(a)
     elif a.config == "batched":
         run_batched(a)
+    elif a.config == "grid64":
+        run_grid64(a)
+    elif a.config == "irregular":
+        run_irregular(a)
     else:
         run_ours(a)
 

@@ -45,6 +45,10 @@ extern "C" {
 /* materials: warp/fem/_arap.py, warp/fem/_stable_neo_hookean.py */
 #define AGB_ARAP 0
 #define AGB_STABLE_NEO_HOOKEAN 1
+/* stable Neo-Hookean with an activation prestrain G = F A, A = I + sym(a) per
+ * cell (warp/fem/_stable_neo_hookean_muscle.py:18-114); a = 0 until
+ * agb_fem_set_activation */
+#define AGB_STABLE_NEO_HOOKEAN_MUSCLE 2
 
 /* flags of agb_fem_eval */
 #define AGB_FUN 1u
@@ -102,6 +106,18 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
 int agb_fem_destroy(agb_fem* fem);
 /* tile statistics: n_tiles, n_tile_vertices (host out; any may be NULL) */
 int agb_fem_info(const agb_fem* fem, int32_t* n_tiles, int32_t* n_tile_vertices);
+/* Connectivity as stored after the Morton reorder, tiling and warp-group
+ * colouring: cells_out[4 c + a] = caller point id of stored corner a of the
+ * caller's cell c (corners of a cell may be permuted by the colouring; the
+ * set and the orientation are kept).  tile_color_hash (may be NULL) receives a
+ * hash of the whole tile / group / corner-slot plan, for bit-exactness checks
+ * across builds and machines.  Host only; no reference counterpart. */
+int agb_fem_cells(const agb_fem* fem, int32_t* cells_out, uint32_t* tile_color_hash);
+/* Muscle potentials: set the per-cell activation a (host, n_cells x 6, the
+ * caller's cell order; cell data `activation`, common/attr_name.py:40-44,
+ * utils/_material.py:15-16).  The element records are rebuilt in place, so a
+ * solver over this single potential sees the new activation. */
+int agb_fem_set_activation(agb_fem* fem, const double* activation);
 
 /* WarpPotential methods (warp/fem/_base.py:151-194); accumulate into output.
  *   fun:       output[0] += sum_e Psi_e dV_e                       (_base.py:243-263)
@@ -279,6 +295,12 @@ int agb_solver_adjoint(agb_solver* solver, const void* rhs, void* lam, const agb
  * with cells in the caller's order (device arrays of the fem's precision). */
 int agb_fem_grad_param_vjp(agb_fem* fem, const void* u, const void* w, void* out_mu, void* out_lambda,
                            void* stream);
+/* Muscle potentials: out_activation[6 c + k] += d(w . grad(u))/d a_{c,k}
+ * (device, the fem's precision, caller's cell order), the backward of the
+ * gradient on the activation array that the reference's inverse experiments
+ * optimise (requires_grad=("activation",)). */
+int agb_fem_grad_activation_vjp(agb_fem* fem, const void* u, const void* w, void* out_activation,
+                                void* stream);
 
 #ifdef __cplusplus
 }

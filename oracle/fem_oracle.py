@@ -15,6 +15,8 @@ kernels in double precision (the reference's default, ``JAX_ENABLE_X64``):
 * rotation-variant SVD and polar          -- ``warp/math/_rotation.py:9-22``
 * ARAP                                    -- ``warp/fem/_arap.py:17-76``
 * stable Neo-Hookean                      -- ``warp/fem/_stable_neo_hookean.py:17-103``
+* stable Neo-Hookean muscle (G = F A)     -- ``warp/fem/_stable_neo_hookean_muscle.py:18-114``,
+  ``func/_misc.py:48-53``
 * per-(tet, qp) kernels with dV weighting and clamps -- ``warp/fem/_base.py:243-383``
 * region precompute (dhdX, dV)            -- ``jax/fem/region/_region.py:84-108``
 * DOF map                                 -- ``forward/dof_map/_dof_map.py:30-49``
@@ -219,6 +221,7 @@ def h6_quad(p, dhdX, F):
 class Material(enum.IntEnum):
     ARAP = 0
     STABLE_NEO_HOOKEAN = 1
+    STABLE_NEO_HOOKEAN_MUSCLE = 2
 
 
 def arap_energy_density(F, mu):
@@ -303,6 +306,40 @@ def snh_hess_quad(F, p, dhdX, mu, lam):
     return lam * h3_quad(p, dhdX, G3) + d2 * h5_quad(p, dhdX) + d3 * h6_quad(p, dhdX, F)
 
 
+def activation_mat33(a):
+    """A = I + [[a0, a3, a4], [a3, a1, a5], [a4, a5, a2]]  (``func/_misc.py:48-53``)."""
+    a = np.asarray(a, np.float64)
+    A = np.empty(a.shape[:-1] + (3, 3))
+    A[..., 0, 0], A[..., 1, 1], A[..., 2, 2] = 1.0 + a[..., 0], 1.0 + a[..., 1], 1.0 + a[..., 2]
+    A[..., 0, 1] = A[..., 1, 0] = a[..., 3]
+    A[..., 0, 2] = A[..., 2, 0] = a[..., 4]
+    A[..., 1, 2] = A[..., 2, 1] = a[..., 5]
+    return A
+
+
+def snh_pk1_dir(F, X, mu, lam):
+    """Directional derivative of ``snh_pk1`` at F along X: mu X + lambda (g3:X) g3 + d3 dg3[X]."""
+    G3 = g3(F)
+    d3 = -mu + lam * (I3(F) - 1.0)
+    return (mu[..., None, None] * X + (lam * ddot(G3, X))[..., None, None] * G3
+            + d3[..., None, None] * _h6_mat(F, X))
+
+
+def muscle_activation_vjp(F, W0, A, mu, lam):
+    """d/da [P(F A) A^T : W0] for one cell (mu, lambda already times dV), with
+    W0 = sum_a w_a dhdX_a^T.  With G = F A, W' = W0 A, P = snh_pk1(G):
+    d/dA = A^-1 (G^T dP[W'] + W'^T P) (A symmetric), and
+    d/da = (Z00, Z11, Z22, Z01 + Z10, Z02 + Z20, Z12 + Z21)."""
+    G = F @ A
+    Wp = W0 @ A
+    P = snh_pk1(G, mu, lam)
+    dP = snh_pk1_dir(G, Wp, mu, lam)
+    T = np.swapaxes(G, -1, -2) @ dP + np.swapaxes(Wp, -1, -2) @ P
+    Z = np.linalg.solve(A, T)
+    return np.stack([Z[..., 0, 0], Z[..., 1, 1], Z[..., 2, 2], Z[..., 0, 1] + Z[..., 1, 0],
+                     Z[..., 0, 2] + Z[..., 2, 0], Z[..., 1, 2] + Z[..., 2, 1]], axis=-1)
+
+
 # ---------------------------------------------------------------------------
 # region precompute (jax/fem/region/_region.py:84-108, element/_tetra.py:37-45)
 # ---------------------------------------------------------------------------
@@ -338,29 +375,52 @@ class FemPotential:
     lam: np.ndarray | None = None  # (N_t,)
     clamp_hess_diag: bool = True
     clamp_hess_quad: bool = True
+    activation: np.ndarray | None = None  # (N_t, 6), muscle only
 
     @classmethod
-    def from_mesh(cls, material, points, cells, mu, lam=None, fraction=None):
+    def from_mesh(cls, material, points, cells, mu, lam=None, fraction=None, activation=None):
         dhdX, dV = region_compute_grad(points, cells, fraction)
         mu = np.broadcast_to(np.asarray(mu, np.float64), (cells.shape[0],)).copy()
         if lam is not None:
             lam = np.broadcast_to(np.asarray(lam, np.float64), (cells.shape[0],)).copy()
-        return cls(Material(material), np.asarray(cells), dhdX, dV, mu, lam)
+        if activation is not None:
+            activation = np.broadcast_to(np.asarray(activation, np.float64), (cells.shape[0], 6)).copy()
+        return cls(Material(material), np.asarray(cells), dhdX, dV, mu, lam, activation=activation)
+
+    @property
+    def muscle(self) -> bool:
+        return self.material == Material.STABLE_NEO_HOOKEAN_MUSCLE
+
+    def _A(self):
+        a = self.activation if self.activation is not None else np.zeros((self.cells.shape[0], 6))
+        return activation_mat33(a)
 
     def _F(self, u):
         return deformation_gradient(u[self.cells], self.dhdX)
 
-    def energy_density(self, u):
+    def _G_dhdX(self, u):
+        """(F, dhdX) of the energy: the muscle evaluates at G = F A with dhdX A
+        (``_stable_neo_hookean_muscle.py:18-114``)."""
         F = self._F(u)
+        if not self.muscle:
+            return F, self.dhdX
+        A = self._A()
+        return F @ A, self.dhdX @ A
+
+    def energy_density(self, u):
         if self.material == Material.ARAP:
-            return arap_energy_density(F, self.mu)
-        return snh_energy_density(F, self.mu, self.lam)
+            return arap_energy_density(self._F(u), self.mu)
+        G, _ = self._G_dhdX(u)
+        return snh_energy_density(G, self.mu, self.lam)
 
     def pk1(self, u):
-        F = self._F(u)
         if self.material == Material.ARAP:
-            return arap_pk1(F, self.mu)
-        return snh_pk1(F, self.mu, self.lam)
+            return arap_pk1(self._F(u), self.mu)
+        G, _ = self._G_dhdX(u)
+        P = snh_pk1(G, self.mu, self.lam)
+        if self.muscle:
+            P = P @ np.swapaxes(self._A(), -1, -2)  # (dPsi/dI2 g2 + dPsi/dI3 g3) A^T
+        return P
 
     def fun(self, u) -> float:
         """Sum_e Psi_e dV_e  (``_base.py:243-263``)."""
@@ -378,11 +438,11 @@ class FemPotential:
 
     def hess_diag(self, u) -> np.ndarray:
         """max(dV h_diag, 0) scattered  (``_base.py:293-324``)."""
-        F = self._F(u)
+        F, dhdX = self._G_dhdX(u)
         if self.material == Material.ARAP:
-            h = arap_hess_diag(F, self.dhdX, self.mu)
+            h = arap_hess_diag(F, dhdX, self.mu)
         else:
-            h = snh_hess_diag(F, self.dhdX, self.mu, self.lam)
+            h = snh_hess_diag(F, dhdX, self.mu, self.lam)
         h = h * self.dV[:, None, None]
         if self.clamp_hess_diag:
             h = np.maximum(h, 0.0)
@@ -390,21 +450,21 @@ class FemPotential:
 
     def hess_prod(self, u, p) -> np.ndarray:
         """dV H_e p_e scattered  (``_base.py:326-351``)."""
-        F = self._F(u)
+        F, dhdX = self._G_dhdX(u)
         pc = p[self.cells]
         if self.material == Material.ARAP:
-            h = arap_hess_prod(F, pc, self.dhdX, self.mu)
+            h = arap_hess_prod(F, pc, dhdX, self.mu)
         else:
-            h = snh_hess_prod(F, pc, self.dhdX, self.mu, self.lam)
+            h = snh_hess_prod(F, pc, dhdX, self.mu, self.lam)
         return self._scatter(u.shape[0], h * self.dV[:, None, None])
 
     def hess_quad_elems(self, u, p) -> np.ndarray:
-        F = self._F(u)
+        F, dhdX = self._G_dhdX(u)
         pc = p[self.cells]
         if self.material == Material.ARAP:
-            h = arap_hess_quad(F, pc, self.dhdX, self.mu)
+            h = arap_hess_quad(F, pc, dhdX, self.mu)
         else:
-            h = snh_hess_quad(F, pc, self.dhdX, self.mu, self.lam)
+            h = snh_hess_quad(F, pc, dhdX, self.mu, self.lam)
         h = h * self.dV
         if self.clamp_hess_quad:
             h = np.maximum(h, 0.0)
@@ -420,8 +480,8 @@ class FemPotential:
         ``utils/_material.py:34-38``).  grad is linear in mu and lambda:
         SNH P = mu (F - cof F) + lambda (J-1) cof F  (``_stable_neo_hookean.py:30-39``),
         ARAP P = mu (F - R)  (``_arap.py:24-28``)."""
-        F = self._F(u)
-        W = deformation_gradient_jvp(self.dhdX, w[self.cells])  # sum_a w_a (x) dhdX_a
+        F, dhdX = self._G_dhdX(u)
+        W = deformation_gradient_jvp(dhdX, w[self.cells])  # sum_a w_a (x) dhdX_a (muscle: dhdX_a A)
         if self.material == Material.ARAP:
             R, _ = polar_rv(F)
             return ddot(F - R, W) * self.dV, None
@@ -430,6 +490,15 @@ class FemPotential:
         dmu = ddot(F - C, W) * self.dV
         dlam = (J - 1.0) * ddot(C, W) * self.dV
         return dmu, dlam
+
+    def grad_activation_vjp(self, u, w):
+        """d(w . grad(u))/d activation per cell, (N_t, 6): the backward of the
+        muscle grad kernel on ``activation`` (``_stable_neo_hookean_muscle.py:30-39``)."""
+        if not self.muscle:
+            raise ValueError("not a muscle potential")
+        F = self._F(u)
+        W0 = deformation_gradient_jvp(self.dhdX, w[self.cells])
+        return muscle_activation_vjp(F, W0, self._A(), self.mu * self.dV, self.lam * self.dV)
 
 
 @dataclasses.dataclass
@@ -706,6 +775,12 @@ def equilibrium_param_grad(model: Model, potential: FemPotential, u: np.ndarray,
     lam = adjoint_dense(model, u, dLdu)
     dmu, dlam = potential.grad_param_vjp(u, lam)
     return -dmu, (None if dlam is None else -dlam), lam
+
+
+def equilibrium_activation_grad(model: Model, potential: FemPotential, u: np.ndarray, dLdu: np.ndarray):
+    """dL/d activation = -d(lam . g)/d activation with H lam = dL/du (muscle)."""
+    lam = adjoint_dense(model, u, dLdu)
+    return -potential.grad_activation_vjp(u, lam), lam
 
 
 # ---------------------------------------------------------------------------
