@@ -1077,7 +1077,7 @@ int agb_fem_grad_param_vjp(agb_fem* f, const void* u, const void* w, void* out_m
   RC(check_launch(launch_pack(f->precision, np, f->space->d_user_of_internal, u, f->d_u, w, f->d_p, s),
                   "pack"));
   RC(check_launch(launch_param_vjp(f->view(), f->precision, f->d_u, f->d_p, f->d_vol, f->d_elem_user,
-                                   out_mu, f->material == AGB_STABLE_NEO_HOOKEAN ? out_lambda : nullptr, s),
+                                   out_mu, f->material != AGB_ARAP ? out_lambda : nullptr, s),
                   "param_vjp"));
   return AGB_OK;
 }

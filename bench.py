@@ -420,6 +420,11 @@ def run_adjoint(a) -> None:
     gradient(p32, theta)  # warm-up (graph capture, kernel attributes)
     L32, d32, t32, s32 = gradient(p32, theta)
     L64, d64, t64, s64 = gradient(p64, theta)
+    # central differences of FP64 forwards solved to 1e-12: one cell's
+    # dL/dtheta moves L by ~1e-9 of itself at h = 1e-4 theta, below what a
+    # 1e-10 forward resolves
+    crit_fd = ag.ConvergenceCriteria(max_steps=400000, rtol=1e-12)
+    p_fd = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float64, criteria=crit_fd)
     cells = rng.choice(m.n_cells, size=min(a.fd_cells, m.n_cells), replace=False)
     fd = []
     t_fd0 = time.perf_counter()
@@ -429,10 +434,18 @@ def run_adjoint(a) -> None:
         for sgn in (1.0, -1.0):
             th = theta.copy()
             th[c] += sgn * h
-            vals.append(loss(p64.solve(mu0 * th, lam)))
+            vals.append(loss(p_fd.solve(mu0 * th, lam)))
         fd.append((vals[0] - vals[1]) / (2 * h))
     t_fd = time.perf_counter() - t_fd0
     fd = np.asarray(fd)
+    # directional derivative along a random direction v over all cells
+    v = rng.normal(size=m.n_cells)
+    hd = 1e-4
+    lp = loss(p_fd.solve(mu0 * theta * (1.0 + hd * v), lam))
+    lm = loss(p_fd.solve(mu0 * theta * (1.0 - hd * v), lam))
+    fd_dir = (lp - lm) / (2 * hd)
+    dir32 = float(np.dot(d32, v * theta))
+    dir64 = float(np.dot(d64, v * theta))
 
     def rel(x, y):
         return float(np.linalg.norm(x - y) / np.linalg.norm(y))
@@ -444,13 +457,16 @@ def run_adjoint(a) -> None:
         "config": {"workload": ADJ_WORKLOAD if not a.small else "snh_grid_6x6x12_adjoint", "n_tets": m.n_cells,
                    "n_vertices": m.n_points, "n_params": m.n_cells, "E": E_MOD, "nu": NU,
                    "loss": "0.5 ||u_surface - u_target||^2, u_target from hidden theta*",
-                   "forward_rtol_f32": 1e-7, "cg_rtol_f32": 1e-6, "fd_step": "1e-4 theta (FP64 forward)"},
+                   "forward_rtol_f32": 1e-7, "cg_rtol_f32": 1e-6,
+                   "fd_step": "1e-4 theta (FP64 forwards to 1e-12)"},
         "f32": {"forward_s": fwd32, "forward_iters": s32.forward.n_steps, "adjoint_s": adj32,
                 "cg_iters": s32.cg.n_iter, "gradient_s": fwd32 + adj32,
                 "rel_err_vs_fd": rel(d32[cells], fd), "rel_err_vs_f64_adjoint": rel(d32, d64)},
         "f64": {"forward_s": t64["forward"], "forward_iters": s64.forward.n_steps, "adjoint_s": t64["adjoint"],
                 "cg_iters": s64.cg.n_iter, "rel_err_vs_fd": rel(d64[cells], fd)},
         "fd": {"cells": int(len(cells)), "seconds": t_fd, "seconds_per_param": t_fd / max(len(cells), 1)},
+        "directional": {"fd": fd_dir, "f32": dir32, "f64": dir64, "rel_err_f32": abs(dir32 - fd_dir) / abs(fd_dir),
+                        "rel_err_f64": abs(dir64 - fd_dir) / abs(fd_dir)},
         "adjoint_vs_plain": {
             "plain": "central differences of the plain forward, 2 solves per parameter",
             "plain_s_all_params_f32_est": 2 * m.n_cells * fwd32,
@@ -464,6 +480,7 @@ def run_adjoint(a) -> None:
 
 
 BATCH_WORKLOAD = "snh_batch_512_grids_4to40_cells_per_axis"
+IRR_MAX_STEPS = 20000
 
 
 def _batch_models(cases, dtype, tile_elems=0, workers=16):
@@ -717,7 +734,7 @@ def run_irregular(a) -> None:
     mask[pts[:, 2] < -0.9] = True  # a fixed cap
     mesh.point_data["FixedMask"] = mask
     mesh.point_data["FixedValue"] = np.zeros((pts.shape[0], 3))
-    f = meshgen.lumped_gravity(mesh, 1000.0) * 100.0
+    f = meshgen.lumped_gravity(mesh, 1000.0)
     b = ag.ModelBuilder()
     b.add_vertices(mesh)
     b.add_fixed(mesh)
@@ -739,17 +756,17 @@ def run_irregular(a) -> None:
     stored, h1 = pot.stored_cells()
     _, h2 = ag.StableNeoHookean.from_pyvista(mesh).stored_cells()
     exact = bool(np.array_equal(np.sort(stored, axis=1), np.sort(cells, axis=1)))
-    sol, t_solve, _ = _solve_case(model, u0, 1e-6, 5000, dev)
+    sol, t_solve, _ = _solve_case(model, u0, 1e-6, IRR_MAX_STEPS, dev)
     nt, ntv = pot.info()
     line = {"metric": "PNCG iters/s on the irregular Delaunay ball",
             "config": {"workload": "snh_delaunay_ball_320k_points" if not a.small else "snh_delaunay_ball_small",
                        "n_tets": int(cells.shape[0]), "n_vertices": int(pts.shape[0]), "mu": "log-uniform [1e3, 1e6]",
-                       "lambda": "10 mu", "load": "100 g body force, cap z < -0.9 fixed"},
+                       "lambda": "10 mu", "load": "gravity (rho 1000, g 9.8), cap z < -0.9 fixed"},
             "iters_per_s": 300 / (tot / 1e3), "ms_per_iter_median": med,
             "hbm_gbs_algorithmic": (64 * cells.shape[0] + 84 * pts.shape[0]) * 300 / (tot / 1e3) / 1e9,
             "tiles": nt, "tile_vertices_per_vertex": ntv / pts.shape[0],
             "connectivity_exact": exact, "plan_hash": h1, "plan_rebuild_identical": h1 == h2, "mesh_s": t_mesh,
-            "solve": {"rtol": 1e-6, "max_steps": 5000, "result": sol.result.name, "iters": sol.n_steps,
+            "solve": {"rtol": 1e-6, "max_steps": IRR_MAX_STEPS, "result": sol.result.name, "iters": sol.n_steps,
                       "seconds": t_solve, "rel_grad": sol.grad_norm / sol.grad_norm_first}}
     print(json.dumps(line), flush=True)
 
