@@ -27,7 +27,7 @@ import torch
 
 from . import meshgen
 from .fem import StableNeoHookean, StableNeoHookeanMuscle, WarpPotentialFem
-from .forward import Forward
+from .forward import Forward, ModelState
 from .model import ModelBuilder
 from .pncg import PNCG, CgSolution, ConvergenceCriteria, Result, Solution
 from .potential import ExternalForce
@@ -78,12 +78,13 @@ class MaterialEquilibrium:
     def muscle(self) -> bool:
         return issubclass(self.material, StableNeoHookeanMuscle)
 
-    def solve(self, mu, lam=None, activation=None) -> torch.Tensor:
+    def solve(self, mu, lam=None, activation=None, u0: torch.Tensor | None = None) -> torch.Tensor:
         """Forward: the converged displacement (n_points, 3) for these cell
-        materials (``activation`` (n_cells, 6): muscle only).  When only the
+        materials (``activation`` (n_cells, 6): muscle only), from zero free
+        displacement or from ``u0`` (its free components; a warm start, as an
+        optimisation loop takes from its previous iterate).  When only the
         activation changed since the last call, the resident device model is
-        kept (new activation records, same tiles and solver) and the solve
-        restarts from zero free displacement."""
+        kept (new activation records, same tiles and solver)."""
         t0 = time.perf_counter()
         act = None
         if self.muscle:
@@ -97,7 +98,7 @@ class MaterialEquilibrium:
             pot, sv, _, model = self._state
             pot.set_activation(act)
             opt = self._opt
-            fwd = Forward(model, opt)
+            fwd = Forward(model, opt, self._initial_state(model, u0))
             torch.cuda.synchronize()
             t1 = time.perf_counter()
             sol = fwd.step()
@@ -127,7 +128,7 @@ class MaterialEquilibrium:
             b.add_potential(ExternalForce.from_pyvista(fm, dtype=self.dtype))
         model = b.finalize()
         opt = PNCG(self.criteria)
-        fwd = Forward(model, opt)
+        fwd = Forward(model, opt, self._initial_state(model, u0))
         opt.solver(fwd.problem)  # device set-up outside the timed solve
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -141,6 +142,13 @@ class MaterialEquilibrium:
         self.stats = AdjointStats(sol)
         self.timings = {"build": t1 - t0, "forward": t2 - t1}
         return u
+
+    def _initial_state(self, model, u0):
+        if u0 is None:
+            return None
+        dm = model.dof_map
+        u0 = u0.to(dtype=model.dtype, device=dm.free_indices.device).reshape(-1, 3)
+        return ModelState(u=dm.to_full(dm.to_free(u0)))
 
     def vjp(self, grad_u: torch.Tensor) -> dict:
         """dL/dmu (and dL/dlambda; dL/dactivation for the muscle) per cell for

@@ -55,11 +55,13 @@ def _args():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
-    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular"], default="plain",
+    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular", "hbm-sizes"],
+                    default="plain",
                     help="plain: the headline PNCG line; adjoint: the 138k-tet adjoint workload; "
                          "batched: 512 uneven meshes in one batch vs solved one by one; grid64: the "
                          "64x64x96 grid (ARAP and stable Neo-Hookean, FP32 and FP64); irregular: the "
-                         "Delaunay ball")
+                         "Delaunay ball; hbm-sizes: cold-L2 read / copy bandwidth of plain torch kernels "
+                         "vs transfer size (the achievable bandwidth of one pass of a given size)")
     ap.add_argument("--n-meshes", type=int, default=512, help="batched: number of meshes")
     ap.add_argument("--fd-cells", type=int, default=32, help="adjoint: cells checked by central differences")
     ap.add_argument("--profile", action="store_true",
@@ -420,11 +422,24 @@ def run_adjoint(a) -> None:
     gradient(p32, theta)  # warm-up (graph capture, kernel attributes)
     L32, d32, t32, s32 = gradient(p32, theta)
     L64, d64, t64, s64 = gradient(p64, theta)
-    # central differences of FP64 forwards solved to 1e-12: one cell's
-    # dL/dtheta moves L by ~1e-9 of itself at h = 1e-4 theta, below what a
-    # 1e-10 forward resolves
-    crit_fd = ag.ConvergenceCriteria(max_steps=400000, rtol=1e-12)
+    # central differences of FP64 forwards: one cell's dL/dtheta moves L by
+    # ~1e-9 of itself at h = 1e-4 theta, so every perturbed solve starts from
+    # the base u* and stops at the same absolute gradient norm (1e-12 of the
+    # cold-start gradient), which keeps the solver's residual error equal on
+    # both sides of each difference
+    g_first = s64.forward.grad_norm_first
+    crit_fd = ag.ConvergenceCriteria(max_steps=400000, rtol=0.0, atol=1e-12 * g_first)
     p_fd = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float64, criteria=crit_fd)
+    u_base = p_fd.solve(mu0 * theta, lam, u0=p64.solve(mu0 * theta, lam)).clone()
+    base_stats = p_fd.stats.forward
+    fd_solves = []
+
+    def fd_loss(th):
+        val = loss(p_fd.solve(mu0 * th, lam, u0=u_base))
+        st = p_fd.stats.forward
+        fd_solves.append((st.result.name, st.n_steps, st.grad_norm))
+        return val
+
     cells = rng.choice(m.n_cells, size=min(a.fd_cells, m.n_cells), replace=False)
     fd = []
     t_fd0 = time.perf_counter()
@@ -434,16 +449,21 @@ def run_adjoint(a) -> None:
         for sgn in (1.0, -1.0):
             th = theta.copy()
             th[c] += sgn * h
-            vals.append(loss(p_fd.solve(mu0 * th, lam)))
+            vals.append(fd_loss(th))
         fd.append((vals[0] - vals[1]) / (2 * h))
     t_fd = time.perf_counter() - t_fd0
     fd = np.asarray(fd)
     # directional derivative along a random direction v over all cells
     v = rng.normal(size=m.n_cells)
     hd = 1e-4
-    lp = loss(p_fd.solve(mu0 * theta * (1.0 + hd * v), lam))
-    lm = loss(p_fd.solve(mu0 * theta * (1.0 - hd * v), lam))
+    lp = fd_loss(theta * (1.0 + hd * v))
+    lm = fd_loss(theta * (1.0 - hd * v))
     fd_dir = (lp - lm) / (2 * hd)
+    from collections import Counter
+    fd_summary = {"base": [base_stats.result.name, base_stats.n_steps, base_stats.grad_norm / g_first],
+                  "results": dict(Counter(r for r, _, _ in fd_solves)),
+                  "max_rel_grad": max(gn for _, _, gn in fd_solves) / g_first,
+                  "mean_steps": float(np.mean([n for _, n, _ in fd_solves])), "loss": L64}
     dir32 = float(np.dot(d32, v * theta))
     dir64 = float(np.dot(d64, v * theta))
 
@@ -458,13 +478,14 @@ def run_adjoint(a) -> None:
                    "n_vertices": m.n_points, "n_params": m.n_cells, "E": E_MOD, "nu": NU,
                    "loss": "0.5 ||u_surface - u_target||^2, u_target from hidden theta*",
                    "forward_rtol_f32": 1e-7, "cg_rtol_f32": 1e-6,
-                   "fd_step": "1e-4 theta (FP64 forwards to 1e-12)"},
+                   "fd_step": "1e-4 theta (FP64 forwards from u*, to 1e-12 of the cold-start gradient)"},
         "f32": {"forward_s": fwd32, "forward_iters": s32.forward.n_steps, "adjoint_s": adj32,
                 "cg_iters": s32.cg.n_iter, "gradient_s": fwd32 + adj32,
                 "rel_err_vs_fd": rel(d32[cells], fd), "rel_err_vs_f64_adjoint": rel(d32, d64)},
         "f64": {"forward_s": t64["forward"], "forward_iters": s64.forward.n_steps, "adjoint_s": t64["adjoint"],
                 "cg_iters": s64.cg.n_iter, "rel_err_vs_fd": rel(d64[cells], fd)},
-        "fd": {"cells": int(len(cells)), "seconds": t_fd, "seconds_per_param": t_fd / max(len(cells), 1)},
+        "fd": {"cells": int(len(cells)), "seconds": t_fd, "seconds_per_param": t_fd / max(len(cells), 1),
+               "solves": fd_summary},
         "directional": {"fd": fd_dir, "f32": dir32, "f64": dir64, "rel_err_f32": abs(dir32 - fd_dir) / abs(fd_dir),
                         "rel_err_f64": abs(dir64 - fd_dir) / abs(fd_dir)},
         "adjoint_vs_plain": {
@@ -577,6 +598,12 @@ def run_batched(a) -> None:
     ok = sum(s.result == ag.Result.PRIMARY_SUCCESS for s in sols)
     ok_plain = sum(s.result == ag.Result.PRIMARY_SUCCESS for s in plain_sols)
     tet_iters = sum(m.n_cells * s.n_steps for (m, _), s in zip(cases, sols))
+    conv = [k for k in range(n) if sols[k].result == ag.Result.PRIMARY_SUCCESS
+            and plain_sols[k].result == ag.Result.PRIMARY_SUCCESS]
+    err_bp_conv = max((float((us[k].double() - plain_u[k].double()).abs().max()) / diag[k] for k in conv),
+                      default=None)
+    stalled = [sols[k].grad_norm / sols[k].grad_norm_first for k in range(n)
+               if sols[k].result != ag.Result.PRIMARY_SUCCESS]
     line = {
         "metric": "batched vs plain: seconds to solve every mesh to ||g||/||g0|| <= 1e-6",
         "config": {"workload": BATCH_WORKLOAD if not a.small else "snh_batch_24_grids_4to12", "n_meshes": n,
@@ -587,6 +614,8 @@ def run_batched(a) -> None:
         "iters": {"mean": float(iters.mean()), "max": int(iters.max()), "min": int(iters.min())},
         "converged": {"batched": int(ok), "plain": int(ok_plain), "of": n},
         "max_diff_batched_vs_plain_over_diag": err_bp,
+        "max_diff_batched_vs_plain_over_diag_converged": err_bp_conv,
+        "not_converged_rel_grad_quantiles": (np.quantile(stalled, [0.0, 0.5, 1.0]).tolist() if stalled else None),
         "max_err_vs_fp64_oracle_over_diag": max(err_o) if err_o else None,
         "autotune": {"seconds": t_tune, "table_ms_per_iter": tune.table}, "build_s": t_build,
         "dtype": "f32", "data": "synthetic",
@@ -771,6 +800,50 @@ def run_irregular(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_hbm_sizes(a) -> None:
+    """Cold-L2 bandwidth of a plain read (torch sum) and copy (torch copy_) vs
+    the bytes one launch moves: a launch of ~100 MB cannot reach the STREAM
+    figure measured on GB-sized arrays (launch latency, ramp-up and drain
+    are a fixed cost of each launch), which bounds what one solver pass of
+    that size can reach."""
+    import statistics
+
+    import torch
+
+    dev = torch.device("cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    rows = []
+    for mb in (16, 45, 72, 100, 200, 500, 2000):
+        n = mb * (1 << 20) // 4
+        x = torch.ones(n, dtype=torch.float32, device=dev)
+        y = torch.empty(n // 2, dtype=torch.float32, device=dev)
+        out = {"mb": mb}
+        for kind in ("read", "copy"):
+            ts = []
+            for r in range(9):
+                flush.fill_(r)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                if kind == "read":
+                    x.sum()
+                else:
+                    y.copy_(x[: n // 2])
+                e1.record()
+                torch.cuda.synchronize()
+                if r >= 2:
+                    ts.append(e0.elapsed_time(e1) * 1e3)
+            us = statistics.median(ts)
+            out[kind + "_us"] = round(us, 2)
+            out[kind + "_gbs"] = round(mb * (1 << 20) / (us * 1e-6) / 1e9, 1)
+        rows.append(out)
+        del x, y
+    peak, kind = _measured_peak()
+    print(json.dumps({"metric": "cold-L2 bandwidth vs bytes per launch", "peak_gbs": peak, "peak_kind": kind,
+                      "rows": rows, "note": "read = sum of a float32 array; copy = half the bytes read, half "
+                                            "written; CUDA events around one launch, 256 MiB flush before each"}),
+          flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
@@ -781,6 +854,8 @@ def main():
         run_batched(a)
     elif a.config == "grid64":
         run_grid64(a)
+    elif a.config == "hbm-sizes":
+        run_hbm_sizes(a)
     elif a.config == "irregular":
         run_irregular(a)
     else:
