@@ -113,6 +113,7 @@ _SIGNATURES = {
     "agb_solver_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(CgParams), POINTER(CgStats), c_void_p]),
     "agb_fem_grad_param_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_set_activation": (c_int, [c_void_p, c_void_p]),
+    "agb_solver_step_kernels": (c_int, [c_void_p, POINTER(c_int32)]),
     "agb_fem_grad_activation_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 

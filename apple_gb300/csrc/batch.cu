@@ -172,19 +172,24 @@ __global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchAr
 }
 
 // reference-state refresh of the models that asked for one (FP32)
+// (grid-stride over tiles / chunks with a resident-sized grid)
 __global__ void __launch_bounds__(kGradThreads) batch_ref_elem_kernel(BatchArgs b) {
   pdl_trigger();
   pdl_wait();
-  if (!b.st[b.tile_mesh[blockIdx.x]].refresh) return;
-  ref_tile<AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x);
+  for (int tile = blockIdx.x; tile < b.a.fv.n_tiles; tile += gridDim.x) {
+    if (!b.st[b.tile_mesh[tile]].refresh) continue;  // uniform across the CTA
+    ref_tile<AGB_STABLE_NEO_HOOKEAN>(b.a, tile);
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(kVThreads) batch_ref_vertex_kernel(BatchArgs b) {
   pdl_trigger();
   pdl_wait();
-  const int c = blockIdx.x;
-  if (!b.st[b.chunk_mesh[c]].refresh) return;
-  for (int i = b.chunk_v0[c] + threadIdx.x; i < b.chunk_v0[c + 1]; i += blockDim.x) ref_vertex(b.a, i);
+  for (int c = blockIdx.x; c < b.n_chunks; c += gridDim.x) {
+    if (!b.st[b.chunk_mesh[c]].refresh) continue;
+    for (int i = b.chunk_v0[c] + threadIdx.x; i < b.chunk_v0[c + 1]; i += blockDim.x) ref_vertex(b.a, i);
+  }
 }
 
 __global__ void batch_force_refresh_kernel(BatchArgs b) {
@@ -270,8 +275,10 @@ cudaError_t launch_pdl_b(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cu
 }
 
 cudaError_t batch_refresh(const BatchArgs& b, cudaStream_t s) {
-  cudaError_t e = launch_pdl_b(batch_ref_elem_kernel, dim3(b.a.fv.n_tiles), dim3(kGradThreads), ref_smem_bytes(), s, b);
-  if (e == cudaSuccess) e = launch_pdl_b(batch_ref_vertex_kernel, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
+  cudaError_t e = launch_pdl_b(batch_ref_elem_kernel, dim3(ref_blocks(b.a.fv.n_tiles)), dim3(kGradThreads),
+                               ref_smem_bytes(), s, b);
+  const int vb = b.n_chunks < kSMs * 8 ? b.n_chunks : kSMs * 8;
+  if (e == cudaSuccess) e = launch_pdl_b(batch_ref_vertex_kernel, dim3(vb > 0 ? vb : 1), dim3(kVThreads), 0, s, b);
   return e;
 }
 

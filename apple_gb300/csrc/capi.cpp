@@ -859,9 +859,19 @@ static int build_step_graph(agb_solver* sv) {
   cudaGraph_t g = nullptr;
   AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
   cudaError_t e = capture_iteration(sv, g, 0ull);
+  size_t n_nodes = 0;
+  if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &n_nodes);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->step_exec, g, 0);
   cudaGraphDestroy(g);
+  sv->step_kernels = (int)n_nodes;
   return check_launch(e, "solver step graph");
+}
+
+int agb_solver_step_kernels(agb_solver* sv, int32_t* n_kernels) {
+  AGB_REQUIRE(sv && n_kernels, AGB_E_INVALID, "agb_solver_step_kernels: null argument");
+  if (!sv->step_exec) RC(build_step_graph(sv));
+  *n_kernels = sv->step_kernels;
+  return AGB_OK;
 }
 
 int agb_solver_iterate(agb_solver* sv, int32_t n_steps, void* stream) {

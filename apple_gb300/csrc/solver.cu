@@ -39,7 +39,7 @@ namespace agb {
 // CTAs as are resident at once (152 SMs x CTAs per SM) and stride over
 // vertices / tiles, so each CTA's block reduction covers several vertices
 // or tiles and the completion sums a few hundred partials in one level.
-constexpr int kVertexCtasPerSM = 4;
+constexpr int kVertexCtasPerSM = 2;
 constexpr int kDirCtasPerSM = 3;
 
 int solver_vertex_blocks(int n_points) {
@@ -297,12 +297,17 @@ __global__ void __launch_bounds__(256) solver_energy_kernel(SolveArgs a) {
 // refresh of the reference state (FP32 stable Neo-Hookean); in the iteration
 // graph both follow the vertex pass as programmatic dependents and return at
 // once unless it asked for a refresh
+// (grid-stride over tiles with a resident-sized grid, so that the usual case
+// -- no refresh due -- costs one short wave)
 template <int MAT>
 __global__ void __launch_bounds__(kGradThreads) solver_ref_elem_kernel(SolveArgs a) {
   pdl_trigger();
   pdl_wait();
   if (!a.st->refresh) return;
-  ref_tile<MAT>(a, blockIdx.x);
+  for (int tile = blockIdx.x; tile < a.fv.n_tiles; tile += gridDim.x) {
+    ref_tile<MAT>(a, tile);
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(kVThreads) solver_ref_vertex_kernel(SolveArgs a) {
@@ -564,10 +569,11 @@ cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_
 cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s) {
   if (!a.delta) return cudaSuccess;
   if (!a.xref || !a.gref || a.precision != AGB_F32 || !snh_family(a.fv.material)) return cudaErrorInvalidValue;
+  const dim3 grid(ref_blocks(a.fv.n_tiles));
   cudaError_t e = a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
-                      ? launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN_MUSCLE>, dim3(a.fv.n_tiles),
+                      ? launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN_MUSCLE>, grid,
                                    dim3(kGradThreads), ref_smem_bytes(), s, a)
-                      : launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN>, dim3(a.fv.n_tiles),
+                      : launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN>, grid,
                                    dim3(kGradThreads), ref_smem_bytes(), s, a);
   if (e == cudaSuccess) e = launch_pdl(solver_ref_vertex_kernel, dim3(a.vblocks), dim3(kVThreads), 0, s, a);
   return e != cudaSuccess ? e : cudaGetLastError();

@@ -241,6 +241,7 @@ struct agb_solver {
   // graphs
   cudaGraphExec_t loop_exec = nullptr;
   cudaGraphExec_t step_exec = nullptr;
+  int step_kernels = 0;  // kernel nodes of one iteration
   cudaStream_t capture_stream = nullptr;
 };
 

@@ -561,6 +561,9 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
 __host__ __device__ constexpr size_t ref_smem_bytes() {
   return (size_t)kTileVerts * (size_t)(kGradWarps + 1) * sizeof(V4<double>);
 }
+// grid of the refresh element pass: at most 4 CTAs per SM (40 KB of shared
+// memory each), striding over the tiles
+inline int ref_blocks(int n_tiles) { return n_tiles < kSMs * 4 ? (n_tiles > 0 ? n_tiles : 1) : kSMs * 4; }
 
 template <int MAT>
 __device__ __forceinline__ void ref_tile(const SolveArgs& a, int tile) {

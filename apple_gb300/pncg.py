@@ -132,6 +132,12 @@ class DeviceSolver:
     def step(self) -> None:
         _lib.call("agb_solver_step", self.handle, stream_ptr())
 
+    def step_kernels(self) -> int:
+        """Kernels one iteration launches (the nodes of the step graph)."""
+        n = ctypes.c_int32()
+        _lib.call("agb_solver_step_kernels", self.handle, ctypes.byref(n))
+        return n.value
+
     def read(self, u_out: torch.Tensor | None = None) -> Solution:
         st = _lib.PncgStats()
         _lib.call("agb_solver_read", self.handle, ptr(u_out), ctypes.byref(st), stream_ptr())

@@ -215,6 +215,10 @@ int agb_solver_reset(agb_solver* solver, const void* u, void* stream);
 int agb_solver_iterate(agb_solver* solver, int32_t n_steps, void* stream);
 /* exactly one iteration as a plain graph (benchmark building block) */
 int agb_solver_step(agb_solver* solver, void* stream);
+/* number of kernels one iteration launches (the nodes of agb_solver_step's
+ * graph: the three passes, plus the two reference-state refresh passes when
+ * the FP32 correction is on) */
+int agb_solver_step_kernels(agb_solver* solver, int32_t* n_kernels);
 /* copy u out (device, caller order) and the stats (host); synchronises stream */
 int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
 /* Diagnostics: time each pass of an iteration on its own with CUDA events on
