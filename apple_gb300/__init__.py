@@ -4,7 +4,7 @@ Host side in Python (this package) over hand-written sm_103a CUDA kernels in
 ``libapple_gb300.so`` (C ABI: ``include/apple_gb300.h``).
 """
 
-from . import meshgen
+from . import meshgen, vtu
 from .fem import Arap, Space, StableNeoHookean, StableNeoHookeanMuscle, WarpPotentialFem, with_lame
 from .forward import Forward, ForwardProblem, ModelState
 from .model import DofMap, DofMapBuilder, Model, ModelBuilder, WarpModel
@@ -34,5 +34,6 @@ __all__ = [
     "WarpModel",
     "WarpPotentialFem",
     "meshgen",
+    "vtu",
     "with_lame",
 ]
