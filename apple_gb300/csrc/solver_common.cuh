@@ -283,23 +283,47 @@ __device__ __forceinline__ void vertex_decide(SolverState* st, const double* tot
 
 // One vertex of the vertex pass: x <- x + t p (float-float), g and d from the
 // vertex's slots s0..s1 (fixed order), external force, DOF mask; the 12 sums
-// of vertex_decide accumulate into s.
+// of vertex_decide accumulate into s.  vertex_load issues the vertex's
+// independent loads, vertex_finish reads its slots and does the rest.
+// (Loading vertex i+1 before finishing vertex i was measured slower: the
+// kernel then runs at its 128-register cap with spills.)
+template <class R>
+struct VertexIn {
+  V4<R> x, xl, g, p, r, f;
+  int s0, s1;
+};
+
 template <class R, bool DELTA>
-__device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0, int s1, R t, const V4<R>* P,
+__device__ __forceinline__ void vertex_load(const SolveArgs& a, int i, int s0, int s1, const V4<R>* P,
+                                            VertexIn<R>& in) {
+  const V4<R>* XA = (const V4<R>*)a.xa;
+  const V4<R>* GD = (const V4<R>*)a.gd;
+  const V4<R>* F = (const V4<R>*)a.force;
+  in.x = XA[2 * i];
+  in.xl = XA[2 * i + 1];
+  in.g = GD[2 * i];
+  in.p = ldg4(P + i);
+  if constexpr (DELTA) in.r = ldg4((const V4<R>*)a.gref + i);
+  if (F) in.f = ldg4(F + i);
+  in.s0 = s0;
+  in.s1 = s1;
+}
+
+template <class R, bool DELTA>
+__device__ __forceinline__ void vertex_finish(const SolveArgs& a, int i, const VertexIn<R>& in, R t,
                                               R (&s)[12]) {
   V4<R>* XA = (V4<R>*)a.xa;
   V4<R>* GD = (V4<R>*)a.gd;
-  const V4<R>* F = (const V4<R>*)a.force;
+  const bool ext = a.force != nullptr;
   const V4<R>* slots = (const V4<R>*)a.slots;
-  const V4<R> x = XA[2 * i], xl = XA[2 * i + 1], g = GD[2 * i], pv = ldg4(P + i);
-  const int mask = (int)x.w;
-  const R p[3] = {pv.x, pv.y, pv.z};
-  R xh[3] = {x.x, x.y, x.z}, xlo[3] = {xl.x, xl.y, xl.z};
+  const int mask = (int)in.x.w;
+  const R p[3] = {in.p.x, in.p.y, in.p.z};
+  R xh[3] = {in.x.x, in.x.y, in.x.z}, xlo[3] = {in.xl.x, in.xl.y, in.xl.z};
 #pragma unroll
   for (int c = 0; c < 3; ++c) pair_add(xh[c], xlo[c], mul_rn(t, p[c]));
   const R xn[3] = {xh[0] + xlo[0], xh[1] + xlo[1], xh[2] + xlo[2]};
   R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
-  for (int k = s0; k < s1; ++k) {
+  for (int k = in.s0; k < in.s1; ++k) {
     const V4<R> sg = slots[2 * k], sd = slots[2 * k + 1];
     gs[0] += sg.x;
     gs[1] += sg.y;
@@ -310,22 +334,17 @@ __device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0,
   }
   if constexpr (DELTA) {
     // g = g(x_ref) + sum_e (f_e(x) - f_e(x_ref)); the force is folded into g(x_ref)
-    const V4<R> r = ldg4((const V4<R>*)a.gref + i);
-    gs[0] += r.x;
-    gs[1] += r.y;
-    gs[2] += r.z;
-    if (F) {
-      const V4<R> f = ldg4(F + i);
-      s[11] += -(f.x * xn[0] + f.y * xn[1] + f.z * xn[2]);
-    }
-  } else if (F) {
-    const V4<R> f = ldg4(F + i);
-    gs[0] -= f.x;
-    gs[1] -= f.y;
-    gs[2] -= f.z;
-    s[11] += -(f.x * xn[0] + f.y * xn[1] + f.z * xn[2]);
+    gs[0] += in.r.x;
+    gs[1] += in.r.y;
+    gs[2] += in.r.z;
+    if (ext) s[11] += -(in.f.x * xn[0] + in.f.y * xn[1] + in.f.z * xn[2]);
+  } else if (ext) {
+    gs[0] -= in.f.x;
+    gs[1] -= in.f.y;
+    gs[2] -= in.f.z;
+    s[11] += -(in.f.x * xn[0] + in.f.y * xn[1] + in.f.z * xn[2]);
   }
-  const R go[3] = {g.x, g.y, g.z};
+  const R go[3] = {in.g.x, in.g.y, in.g.z};
   R gn[3], dn[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -351,10 +370,18 @@ __device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0,
     s[9] += p[c] * gn[c];
     s[10] += gn[c] * gn[c];
   }
-  XA[2 * i] = V4<R>{xh[0], xh[1], xh[2], x.w};
+  XA[2 * i] = V4<R>{xh[0], xh[1], xh[2], in.x.w};
   XA[2 * i + 1] = V4<R>{xlo[0], xlo[1], xlo[2], R(0)};
   GD[2 * i] = V4<R>{gn[0], gn[1], gn[2], R(0)};
   GD[2 * i + 1] = V4<R>{dn[0], dn[1], dn[2], R(0)};
+}
+
+template <class R, bool DELTA>
+__device__ __forceinline__ void vertex_update(const SolveArgs& a, int i, int s0, int s1, R t, const V4<R>* P,
+                                              R (&s)[12]) {
+  VertexIn<R> in;
+  vertex_load<R, DELTA>(a, i, s0, s1, P, in);
+  vertex_finish<R, DELTA>(a, i, in, t, s);
 }
 
 // Whether a solver instantiation uses the reference-state correction: FP32
