@@ -1,7 +1,7 @@
 """Build and load ``oracle/liboracle.so`` (gcc, OpenMP, FP64).
 
 Test infrastructure: the C restatement of the reference path, used as the
-timed CPU baseline and as a second checker.  Portable flags only (the same
+timed CPU baseline and as a second oracle.  Portable flags only (the same
 source builds on the x86 container and the Arm GPU host).
 """
 

@@ -2,7 +2,7 @@
  * C / OpenMP FP64 restatement of the reference's FEM kernels and PNCG loop.
  *
  * TEST INFRASTRUCTURE ONLY: the timed CPU baseline (bench.py cpu_baseline
- * and --impl reference) and a second checker in tests/.  The product never
+ * and --impl reference) and a second oracle in tests/.  The product never
  * links it.
  *
  * Follows, per element and per call, the Warp kernels of liblaf/apple

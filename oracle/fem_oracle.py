@@ -1,6 +1,6 @@
 """FP64 NumPy oracle for the FEM-elasticity / PNCG hot path of liblaf/apple.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+TEST INFRASTRUCTURE ONLY.  This module is the oracle: only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference``
 legs of ``bench.py`` may import it.  The product (``apple_gb300``) never
 imports, calls or links anything under ``oracle/``.

@@ -1,6 +1,6 @@
 """The FP64 oracle of the adjoint path: the material VJP of the gradient and
 the implicit gradient of the equilibrium, both against central differences.
-These pin the checker the GPU adjoint tests compare with."""
+These pin the oracle the GPU adjoint tests compare with."""
 
 import numpy as np
 import pytest
