@@ -80,7 +80,9 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   const V4<R>* pprev = p_prev<R>(a, pb);
   V4<R>* pcur = p_cur<R>(a, pb);
 
-  Acc<R> sums[N] = {};
+  // pHp and c3..c6 in plain R, c2 (terms of both signs) in float-float
+  R plain[N] = {};
+  Acc<R> c2acc = {};
   for (; tile < a.fv.n_tiles; tile += gridDim.x) {
     stage_dir<R>(a, vid, beta, inv_mean, pprev, pcur, sx, sp);
     // the next tile's vertex id, in flight while this tile computes
@@ -111,18 +113,19 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
         snh_prepare(G, s);
         SnhDir<R> d;
         snh_dir(s, dF, d);
-        sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
+        plain[0] += fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0));
         R c[5];
         snh_poly(s, d, geo.mu, geo.lam, c);
+        c2acc.add(c[0]);
 #pragma unroll
-        for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
+        for (int m = 1; m < 5; ++m) plain[1 + m] += c[m];
       } else {
         const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
         Svd<R> sv;
         svd_rv(G, jm1, sv);
         R lk[3];
         arap_lambdas(sv, lk);
-        sums[0].add(fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0)));
+        plain[0] += fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0));
       }
       geo = geon;
       ids = idsn;
@@ -138,6 +141,13 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
     __syncthreads();
   }
   double tot[N];
+  Acc<R> sums[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    sums[k] = Acc<R>{};
+    sums[k].add(plain[k]);
+  }
+  if constexpr (N > 1) sums[1] = c2acc;
   if (!grid_reduce_masked<N, FF, R>(sums, (AccStore<R>*)a.part_a, a.cnt_a, gridDim.x, red, tot)) return;
   if (threadIdx.x != 0) return;
   dir_decide<MAT>(st, tot);
