@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs 
 }
 
 template <class R, bool DELTA>
-__global__ void __launch_bounds__(kGradThreads, 7) batch_grad_kernel(BatchArgs b) {
+__global__ void __launch_bounds__(kGradThreads, 6) batch_grad_kernel(BatchArgs b) {
   grad_tile<R, AGB_STABLE_NEO_HOOKEAN, DELTA>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
 }
 
