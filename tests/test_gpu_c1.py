@@ -5,10 +5,10 @@ vertices, 5,000 tets), stable Neo-Hookean E = 1e4, nu = 0.45, gravity
 Checks, with the FP64 oracle evaluated at the GPU's answers: the FP32 solve
 reaches ||g||/||g0|| <= 1e-6 and is an equilibrium of the FP64 model to 1e-4
 (its output is rounded to FP32); the FP64 solve is one to 1e-7; both land in
-the same equilibrium.  (The gravity load is about E / L here: the cube sags
-by more than its height, through inverted elements, which stable
-Neo-Hookean allows; the FP64 C restatement of the reference loop ends in a
-failed line search near 1e-6 on it.)"""
+the same equilibrium, whose energy the FP64 C restatement of the reference
+loop reaches too (to 1e-9; it ends in a failed line search near 1e-6).  (The
+gravity load is about E / L here: the cube sags by more than its height,
+through inverted elements, which stable Neo-Hookean allows.)"""
 
 import numpy as np
 import pytest
@@ -16,6 +16,7 @@ import torch
 
 import apple_gb300 as ag
 from apple_gb300 import meshgen
+from oracle import build_c
 from oracle import fem_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -60,7 +61,7 @@ def test_c1_cube_fp32_and_fp64_against_the_oracle(cuda_device):
         return np.linalg.norm(om.grad(u)[free]) / g0
 
     sols = {}
-    for dtype, rtol, bound in ((torch.float32, 1e-6, 1e-4), (torch.float64, 1e-9, 1e-7)):
+    for dtype, rtol, bound in ((torch.float32, 1e-6, 1e-4), (torch.float64, 1e-8, 1e-7)):
         fwd = ag.Forward(_model(m, mu, lam, mask, f, dtype),
                          ag.PNCG(ag.ConvergenceCriteria(max_steps=20000, rtol=rtol)))
         sol = fwd.step()
@@ -74,3 +75,10 @@ def test_c1_cube_fp32_and_fp64_against_the_oracle(cuda_device):
     # FP32 and FP64 end in the same equilibrium
     diag = np.linalg.norm(m.points.max(0) - m.points.min(0))
     assert np.abs(sols[torch.float32] - sols[torch.float64]).max() < 1e-3 * diag
+    # ... as the C restatement of the reference loop (FP64): the same energy
+    dhdX, dV = O.region_compute_grad(m.points, m.cells)
+    cm = build_c.CModel(1, m.cells, dhdX, dV, np.full(m.n_cells, mu), np.full(m.n_cells, lam), m.n_points,
+                        mask=mask, force=f)
+    u_c, _ = cm.pncg(np.zeros((m.n_points, 3)), max_steps=20000, rtol=1e-10)
+    e_gpu, e_c = om.fun(sols[torch.float64]), om.fun(u_c)
+    assert abs(e_gpu - e_c) <= 1e-9 * abs(e_c)
