@@ -295,7 +295,7 @@ int agb_solver_adjoint(agb_solver* solver, const void* rhs, void* lam, const agb
  * utils/_material.py:34-38): for a vector field w (device, caller order,
  * n_points x 3) and displacement u,
  *   out_mu[c]     += d(w . grad(u))/d mu_c
- *   out_lambda[c] += d(w . grad(u))/d lambda_c   (stable Neo-Hookean; may be NULL)
+ *   out_lambda[c] += d(w . grad(u))/d lambda_c   (stable Neo-Hookean and its muscle; may be NULL)
  * with cells in the caller's order (device arrays of the fem's precision). */
 int agb_fem_grad_param_vjp(agb_fem* fem, const void* u, const void* w, void* out_mu, void* out_lambda,
                            void* stream);
