@@ -114,6 +114,9 @@ _SIGNATURES = {
     "agb_fem_grad_param_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_set_activation": (c_int, [c_void_p, c_void_p]),
     "agb_solver_step_kernels": (c_int, [c_void_p, POINTER(c_int32)]),
+    "agb_solver_checkpoint_size": (c_int, [c_void_p, POINTER(ctypes.c_size_t)]),
+    "agb_solver_save": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "agb_solver_load": (c_int, [c_void_p, c_void_p, c_void_p]),
     "agb_fem_grad_activation_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 

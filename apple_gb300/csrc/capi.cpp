@@ -918,6 +918,71 @@ int agb_solver_read(agb_solver* sv, void* u_out, agb_pncg_stats* stats, void* st
   return AGB_OK;
 }
 
+// checkpoint layout: header, then xa (2 V4 per vertex), gd (2 V4), p0, p1,
+// [xref, gref when the FP32 correction is on], SolverState
+struct CheckpointHeader {
+  uint64_t magic;
+  int32_t version, precision, n_points, delta, state_bytes, pad;
+};
+constexpr uint64_t kCheckpointMagic = 0x4147424350544b31ull;  // "AGBCPTK1"
+
+static size_t checkpoint_vec_bytes(const agb_solver* sv) {
+  const size_t v4 = v4_bytes(sv->precision) * (size_t)sv->args.n_points;
+  return 2 * v4 + 2 * v4 + v4 + v4 + (sv->args.delta ? 2 * v4 : 0);
+}
+
+int agb_solver_checkpoint_size(agb_solver* sv, size_t* bytes) {
+  AGB_REQUIRE(sv && bytes, AGB_E_INVALID, "agb_solver_checkpoint_size: null argument");
+  *bytes = sizeof(CheckpointHeader) + checkpoint_vec_bytes(sv) + sizeof(SolverState);
+  return AGB_OK;
+}
+
+static std::vector<std::pair<void*, size_t>> checkpoint_arrays(agb_solver* sv) {
+  const size_t v4 = v4_bytes(sv->precision) * (size_t)sv->args.n_points;
+  std::vector<std::pair<void*, size_t>> a = {{sv->d_xa, 2 * v4}, {sv->d_gd, 2 * v4}, {sv->d_p0, v4}, {sv->d_p1, v4}};
+  if (sv->args.delta) {
+    a.push_back({sv->d_xref, v4});
+    a.push_back({sv->d_gref, v4});
+  }
+  a.push_back({(void*)sv->d_state, sizeof(SolverState)});
+  return a;
+}
+
+int agb_solver_save(agb_solver* sv, void* host, void* stream) {
+  AGB_REQUIRE(sv && host, AGB_E_INVALID, "agb_solver_save: null argument");
+  cudaStream_t s = as_stream(stream);
+  CheckpointHeader h{kCheckpointMagic, 1, sv->precision, sv->args.n_points, sv->args.delta,
+                     (int32_t)sizeof(SolverState), 0};
+  std::memcpy(host, &h, sizeof(h));
+  char* dst = static_cast<char*>(host) + sizeof(h);
+  for (const auto& [ptr, n] : checkpoint_arrays(sv)) {
+    AGB_CHECK_CUDA(cudaMemcpyAsync(dst, ptr, n, cudaMemcpyDeviceToHost, s));
+    dst += n;
+  }
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  return AGB_OK;
+}
+
+int agb_solver_load(agb_solver* sv, const void* host, void* stream) {
+  AGB_REQUIRE(sv && host, AGB_E_INVALID, "agb_solver_load: null argument");
+  CheckpointHeader h;
+  std::memcpy(&h, host, sizeof(h));
+  AGB_REQUIRE(h.magic == kCheckpointMagic && h.version == 1, AGB_E_INVALID, "agb_solver_load: not a checkpoint");
+  AGB_REQUIRE(h.precision == sv->precision && h.n_points == sv->args.n_points && h.delta == sv->args.delta &&
+                  h.state_bytes == (int32_t)sizeof(SolverState),
+              AGB_E_INVALID,
+              "agb_solver_load: checkpoint of another solver (precision %d, %d points, correction %d)",
+              h.precision, h.n_points, h.delta);
+  cudaStream_t s = as_stream(stream);
+  const char* src = static_cast<const char*>(host) + sizeof(h);
+  for (const auto& [ptr, n] : checkpoint_arrays(sv)) {
+    AGB_CHECK_CUDA(cudaMemcpyAsync(ptr, src, n, cudaMemcpyHostToDevice, s));
+    src += n;
+  }
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  return AGB_OK;
+}
+
 int agb_solver_time_passes(agb_solver* sv, int32_t reps, void* flush, size_t flush_bytes,
                            float* ms, void* stream) {
   AGB_REQUIRE(sv && ms && reps > 0, AGB_E_INVALID, "agb_solver_time_passes: bad argument");

@@ -132,6 +132,20 @@ class DeviceSolver:
     def step(self) -> None:
         _lib.call("agb_solver_step", self.handle, stream_ptr())
 
+    def save_state(self) -> torch.Tensor:
+        """A checkpoint of the whole PNCG state (uint8 CPU tensor), for
+        :meth:`load_state` on this or an identically built solver."""
+        n = ctypes.c_size_t()
+        _lib.call("agb_solver_checkpoint_size", self.handle, ctypes.byref(n))
+        blob = torch.empty(n.value, dtype=torch.uint8)
+        _lib.call("agb_solver_save", self.handle, ctypes.c_void_p(blob.data_ptr()), stream_ptr())
+        return blob
+
+    def load_state(self, blob: torch.Tensor) -> None:
+        """Restore a checkpoint; the next iterate() continues from it."""
+        blob = blob.to(dtype=torch.uint8, device="cpu").contiguous()
+        _lib.call("agb_solver_load", self.handle, ctypes.c_void_p(blob.data_ptr()), stream_ptr())
+
     def step_kernels(self) -> int:
         """Kernels one iteration launches (the nodes of the step graph)."""
         n = ctypes.c_int32()

@@ -221,6 +221,19 @@ int agb_solver_step(agb_solver* solver, void* stream);
 int agb_solver_step_kernels(agb_solver* solver, int32_t* n_kernels);
 /* copy u out (device, caller order) and the stats (host); synchronises stream */
 int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
+
+/* Checkpoint / resume of a solve (the reference has none; its experiments
+ * restart from saved .vtu states).  A checkpoint is the solver's whole PNCG
+ * state -- positions as float-float pairs, gradient, Hessian diagonal, both
+ * search directions, the reference state of the FP32 correction and the
+ * scalar state -- in a host buffer of agb_solver_checkpoint_size bytes.
+ * agb_solver_load accepts a checkpoint of a solver with the same vertex
+ * count, precision and correction setting (AGB_E_INVALID otherwise); the
+ * next agb_solver_iterate continues the solve exactly where it was saved.
+ * Both synchronise the stream. */
+int agb_solver_checkpoint_size(agb_solver* solver, size_t* bytes);
+int agb_solver_save(agb_solver* solver, void* host, void* stream);
+int agb_solver_load(agb_solver* solver, const void* host, void* stream);
 /* Diagnostics: time each pass of an iteration on its own with CUDA events on
  * `stream`, `reps` launches each (direction, gradient, vertex pass), writing
  * `flush_bytes` of the device buffer `flush` (may be NULL) before every launch

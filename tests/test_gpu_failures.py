@@ -1,0 +1,116 @@
+"""Failure handling and checkpoint / resume of the device PNCG (GB300).
+
+Failures are injected on the host, never by faulting the GPU: a NaN in the
+initial displacement, an exhausted step budget, a model whose free DOFs have
+no stiffness at all, a checkpoint loaded into the wrong solver.  A checkpoint
+taken mid-solve and restored continues bit for bit."""
+
+import numpy as np
+import pytest
+import torch
+
+import apple_gb300 as ag
+from apple_gb300 import meshgen
+from apple_gb300.forward import ModelState
+
+pytestmark = pytest.mark.gpu
+
+
+def _column(n=(4, 4, 6), dtype=torch.float32, extra_points=0, fix_all_mesh=False):
+    m = meshgen.grid(*n)
+    pts = m.points
+    if extra_points:
+        pts = np.concatenate([pts, 5.0 + np.arange(3 * extra_points, dtype=float).reshape(-1, 3)])
+    n_pts = pts.shape[0]
+    lam, mu = meshgen.lame_converter(1e4, 0.45)
+    mesh = ag.with_lame(meshgen.TetMesh(pts, m.cells), mu, lam)
+    mask = np.zeros((n_pts, 3), bool)
+    if fix_all_mesh:
+        mask[: m.n_points] = True
+    else:
+        mask[: m.n_points][meshgen.face_mask(m, 2, "min")] = True
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = np.zeros((n_pts, 3))
+    b = ag.ModelBuilder(dtype=dtype)
+    b.add_vertices(mesh)
+    b.add_fixed(mesh)
+    b.add_potential(ag.StableNeoHookean.from_pyvista(mesh, dtype=dtype))
+    f = np.zeros((n_pts, 3))
+    f[: m.n_points] = meshgen.lumped_gravity(m, 1000.0)
+    fm = meshgen.TetMesh(pts, m.cells)
+    fm.point_data["Force"] = f
+    fm.point_data["GlobalPointId"] = np.arange(n_pts)
+    b.add_potential(ag.ExternalForce.from_pyvista(fm, dtype=dtype))
+    return b.finalize()
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_checkpoint_resume_is_exact(dtype, cuda_device):
+    model = _column(dtype=dtype)
+    opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=10_000, rtol=1e-7))
+    fwd = ag.Forward(model, opt)
+    sv = opt.solver(fwd.problem)
+    sv.reset(fwd.state.u)
+    sv.iterate(15)
+    blob = sv.save_state()
+    sv.iterate(25)
+    u_a = torch.empty_like(fwd.state.u)
+    st_a = sv.read(u_a)
+    sv.load_state(blob)
+    sv.iterate(25)
+    u_b = torch.empty_like(fwd.state.u)
+    st_b = sv.read(u_b)
+    assert st_a.n_steps == st_b.n_steps == 40
+    assert torch.equal(u_a, u_b)
+    assert st_a.grad_norm == st_b.grad_norm
+    # an identically built solver resumes the same way
+    opt2 = ag.PNCG(ag.ConvergenceCriteria(max_steps=10_000, rtol=1e-7))
+    sv2 = opt2.solver(ag.ForwardProblem(model))
+    sv2.load_state(blob)
+    sv2.iterate(25)
+    u_c = torch.empty_like(fwd.state.u)
+    sv2.read(u_c)
+    assert torch.equal(u_a, u_c)
+
+
+def test_checkpoint_rejected_by_another_solver(cuda_device):
+    a, b = _column(n=(4, 4, 6)), _column(n=(4, 4, 7))
+    opt_a, opt_b = ag.PNCG(), ag.PNCG()
+    sa = opt_a.solver(ag.ForwardProblem(a))
+    sa.reset(ag.Forward(a, opt_a).state.u)
+    sb = opt_b.solver(ag.ForwardProblem(b))
+    with pytest.raises(RuntimeError):
+        sb.load_state(sa.save_state())
+    bad = sa.save_state()
+    bad[:8] = 0  # not a checkpoint
+    with pytest.raises(RuntimeError):
+        sa.load_state(bad)
+
+
+def test_nan_input_ends_with_nan_encountered(cuda_device):
+    model = _column()
+    fwd = ag.Forward(model, ag.PNCG(ag.ConvergenceCriteria(max_steps=100, rtol=1e-6)))
+    u = fwd.state.u.clone()
+    free = np.flatnonzero(~model.dof_map.fixed_mask.reshape(-1))
+    u.view(-1)[int(free[-1])] = float("nan")  # a free DOF: the solve starts from it
+    fwd.state = ModelState(u=u)
+    sol = fwd.step()
+    assert sol.result == ag.Result.NAN_ENCOUNTERED, sol
+
+
+def test_step_budget_exhaustion(cuda_device):
+    model = _column()
+    sol = ag.Forward(model, ag.PNCG(ag.ConvergenceCriteria(max_steps=3, rtol=1e-12))).step()
+    assert sol.result == ag.Result.MAX_STEPS_REACHED and sol.n_steps == 3, sol
+
+
+def test_free_dofs_without_stiffness(cuda_device):
+    """Every mesh vertex fixed; the only free DOFs belong to points no cell
+    references: zero gradient and zero diagonal (the preconditioner's mean
+    fallback), so the solve ends at once and moves nothing."""
+    model = _column(extra_points=2, fix_all_mesh=True)
+    fwd = ag.Forward(model, ag.PNCG(ag.ConvergenceCriteria(max_steps=100, rtol=1e-6)))
+    u0 = fwd.state.u.clone()
+    sol = fwd.step()
+    assert sol.result == ag.Result.PRIMARY_SUCCESS, sol
+    assert torch.equal(fwd.state.u, u0)
