@@ -262,12 +262,14 @@ def run_ours(a) -> None:
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
     _barrier(world)
     torch.cuda.synchronize(dev)
+    torch.cuda.nvtx.range_push("steps")  # the timed region, for ncu --nvtx-include "steps/"
     for i in range(a.steps):
         flush.fill_(i & 0xFF)
         ev[i][0].record(stream)
         solver.step()
         ev[i][1].record(stream)
     torch.cuda.synchronize(dev)
+    torch.cuda.nvtx.range_pop()
     _barrier(world)
     clk = clocks.stop()
     step_ms = [s.elapsed_time(e) for s, e in ev]
