@@ -55,13 +55,14 @@ def _args():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
-    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular", "hbm-sizes"],
+    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular", "hbm-sizes", "muscle"],
                     default="plain",
                     help="plain: the headline PNCG line; adjoint: the 138k-tet adjoint workload; "
                          "batched: 512 uneven meshes in one batch vs solved one by one; grid64: the "
                          "64x64x96 grid (ARAP and stable Neo-Hookean, FP32 and FP64); irregular: the "
                          "Delaunay ball; hbm-sizes: cold-L2 read / copy bandwidth of plain torch kernels "
-                         "vs transfer size (the achievable bandwidth of one pass of a given size)")
+                         "vs transfer size (the achievable bandwidth of one pass of a given size); muscle: the "
+                         "headline grid with an activation-prestrained stable Neo-Hookean muscle vs the plain material")
     ap.add_argument("--n-meshes", type=int, default=512, help="batched: number of meshes")
     ap.add_argument("--fd-cells", type=int, default=8,
                     help="adjoint: cells checked by central differences (half random, half largest |dL/dtheta|)")
@@ -818,6 +819,45 @@ def run_irregular(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_muscle(a) -> None:
+    """The headline grid (stretch 30%) as a stable Neo-Hookean muscle with a
+    random per-cell activation (|a| ~ 0.05) vs the same grid without it:
+    PNCG iterations per second, and a solve to 1e-6."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+
+    dev = torch.device("cuda")
+    m, mu, lam, mask, fv = _mesh(a.small)
+    act = 0.05 * np.random.default_rng(0).normal(size=(m.n_cells, 6))
+    u0 = torch.tensor(np.where(mask, fv, 0.0), dtype=torch.float32, device=dev)
+    out = {}
+    for name, cls in (("stable_neo_hookean", ag.StableNeoHookean), ("muscle", ag.StableNeoHookeanMuscle)):
+        mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells), mu, lam)
+        if cls is ag.StableNeoHookeanMuscle:
+            mesh.cell_data["activation"] = act
+        mesh.point_data["FixedMask"] = mask
+        mesh.point_data["FixedValue"] = fv
+        b = ag.ModelBuilder()
+        b.add_vertices(mesh)
+        b.add_fixed(mesh)
+        b.add_potential(cls.from_pyvista(mesh))
+        model = b.finalize()
+        opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=2**30, rtol=0.0))
+        sv = opt.solver(ag.ForwardProblem(model))
+        sv.reset(u0)
+        med, tot = _timed_steps(sv, 300, 5, dev)
+        sol, t_solve, _ = _solve_case(model, u0, 1e-6, 20000, dev)
+        out[name] = {"iters_per_s": 300 / (tot / 1e3), "ms_per_iter_median": med,
+                     "solve": {"rtol": 1e-6, "result": sol.result.name, "iters": sol.n_steps, "seconds": t_solve}}
+    out["muscle_over_plain_time_per_iter"] = out["stable_neo_hookean"]["iters_per_s"] / out["muscle"]["iters_per_s"]
+    print(json.dumps({"metric": "PNCG iters/s, muscle vs plain stable Neo-Hookean",
+                      "config": {"workload": WORKLOAD + ("_small" if a.small else ""), "n_tets": m.n_cells,
+                                 "activation": "N(0, 0.05^2) per component, seed 0"}, **out}), flush=True)
+
+
 def run_hbm_sizes(a) -> None:
     """Cold-L2 bandwidth of a plain read (torch sum) and copy (torch copy_) vs
     the bytes one launch moves: a launch of ~100 MB cannot reach the STREAM
@@ -874,6 +914,8 @@ def main():
         run_grid64(a)
     elif a.config == "hbm-sizes":
         run_hbm_sizes(a)
+    elif a.config == "muscle":
+        run_muscle(a)
     elif a.config == "irregular":
         run_irregular(a)
     else:
