@@ -186,12 +186,13 @@ def _encode(a: np.ndarray, fmt: str, compress: bool, hdr=np.uint64) -> tuple[str
 
 
 def write(path, mesh, point_data: dict | None = None, cell_data: dict | None = None, *,
-          fmt: str = "appended", compress: bool = True) -> None:
+          fmt: str = "appended", compress: bool = True, encoding: str = "raw") -> None:
     """Write points, tetrahedra and arrays (``mesh.point_data`` / ``cell_data``
     merged with the extra dicts) as a ``.vtu``; ``fmt`` is ``ascii``, ``binary``
-    or ``appended`` (raw), ``compress`` zlib-compresses binary data."""
-    if fmt not in ("ascii", "binary", "appended"):
-        raise ValueError(f"unknown format {fmt}")
+    or ``appended``, ``encoding`` (appended data) ``raw`` or ``base64``, and
+    ``compress`` zlib-compresses binary data."""
+    if fmt not in ("ascii", "binary", "appended") or encoding not in ("raw", "base64"):
+        raise ValueError(f"unknown format {fmt} / encoding {encoding}")
     pts = np.asarray(mesh.points, np.float64).reshape(-1, 3)
     cells = np.asarray(mesh.cells, np.int64).reshape(-1, 4)
     pd = dict(getattr(mesh, "point_data", {}) or {})
@@ -221,6 +222,8 @@ def write(path, mesh, point_data: dict | None = None, cell_data: dict | None = N
         if a.ndim > 1:
             el.set("NumberOfComponents", str(int(np.prod(a.shape[1:]))))
         text, blob = _encode(a, fmt, compress)
+        if fmt == "appended" and encoding == "base64":  # the inline form's text, appended
+            blob = _encode(a, "binary", compress)[0].encode("ascii")
         if fmt == "appended":
             el.set("offset", str(pos))
             appended.append(blob)
@@ -245,6 +248,6 @@ def write(path, mesh, point_data: dict | None = None, cell_data: dict | None = N
             f.write(b'<?xml version="1.0"?>\n' + xml.encode())
             return
         head, tail = xml.rsplit("</VTKFile>", 1)
-        f.write(b'<?xml version="1.0"?>\n' + head.encode() + b'<AppendedData encoding="raw">_')
+        f.write(b'<?xml version="1.0"?>\n' + head.encode() + f'<AppendedData encoding="{encoding}">_'.encode())
         f.write(b"".join(appended))
         f.write(b"</AppendedData></VTKFile>" + tail.encode())

@@ -20,14 +20,15 @@ def _arrays(m, rng):
     return pd, cd
 
 
-@pytest.mark.parametrize("fmt", ["ascii", "binary", "appended"])
+@pytest.mark.parametrize("fmt", ["ascii", "binary", "appended", "appended-base64"])
 @pytest.mark.parametrize("compress", [False, True])
 def test_round_trip(tmp_path, fmt, compress):
     rng = np.random.default_rng(0)
     m = meshgen.grid(20, 3, 2)  # > 32 KiB per array: several zlib blocks
     pd, cd = _arrays(m, rng)
     f = tmp_path / "m.vtu"
-    vtu.write(f, m, pd, cd, fmt=fmt, compress=compress)
+    enc = "base64" if fmt.endswith("base64") else "raw"
+    vtu.write(f, m, pd, cd, fmt=fmt.split("-")[0], compress=compress, encoding=enc)
     r = vtu.read(f)
     np.testing.assert_array_equal(r.points, m.points)
     np.testing.assert_array_equal(r.cells, m.cells)
