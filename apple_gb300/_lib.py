@@ -74,6 +74,8 @@ _SIGNATURES = {
     "agb_fem_destroy": (c_int, [c_void_p]),
     "agb_fem_info": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
     "agb_fem_cells": (c_int, [c_void_p, c_void_p, POINTER(ctypes.c_uint32)]),
+    "agb_plan_tiles": (c_int, [c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_int32), POINTER(c_int32),
+                               c_void_p, c_void_p, c_void_p]),
     "agb_fem_fun": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_fem_hess_diag": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

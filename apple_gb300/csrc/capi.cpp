@@ -381,6 +381,48 @@ int agb_fem_info(const agb_fem* f, int32_t* n_tiles, int32_t* n_tv) {
   return AGB_OK;
 }
 
+int agb_plan_tiles(int32_t n_points, int32_t n_cells, const int32_t* cells, const double* points,
+                   int32_t tile_elems, int32_t* n_tiles, int32_t* n_groups, int32_t* tile_of_cell,
+                   int32_t* group_of_cell, int32_t* slot_cells) {
+  AGB_REQUIRE(n_points > 0 && n_cells >= 0 && (n_cells == 0 || cells) && points && tile_elems >= 0 && n_tiles &&
+                  n_groups,
+              AGB_E_INVALID, "agb_plan_tiles: bad arguments");
+  for (int64_t k = 0; k < 4 * (int64_t)n_cells; ++k)
+    AGB_REQUIRE(cells[k] >= 0 && cells[k] < n_points, AGB_E_MESH,
+                "agb_plan_tiles: cell %lld corner %lld has point id %d outside [0, %d)", (long long)(k / 4),
+                (long long)(k % 4), cells[k], n_points);
+  // the same vertex order and element order as agb_space_create + agb_fem_create
+  const std::vector<int32_t> uoi = morton_order(n_points, points);
+  std::vector<int32_t> iou(n_points);
+  for (int i = 0; i < n_points; ++i) iou[uoi[i]] = i;
+  std::vector<int32_t> cells_int(4 * (size_t)n_cells);
+  for (size_t k = 0; k < cells_int.size(); ++k) cells_int[k] = iou[cells[k]];
+  std::vector<double> centroid(3 * (size_t)n_cells), D9(9 * (size_t)n_cells, 0.0), zero(n_cells, 0.0);
+  for (int e = 0; e < n_cells; ++e)
+    for (int c = 0; c < 3; ++c) {
+      double s = 0.0;
+      for (int a = 0; a < 4; ++a) s += points[3 * (size_t)cells[4 * e + a] + c];
+      centroid[3 * (size_t)e + c] = 0.25 * s;
+    }
+  TilePlan P;
+  RC(build_tiles(n_cells, cells_int.data(), centroid.data(), D9.data(), zero.data(), zero.data(), tile_elems, &P));
+  *n_tiles = P.n_tiles;
+  *n_groups = (int32_t)P.group_estart.size() - 1;
+  for (int t = 0; t < P.n_tiles; ++t) {
+    const int vs = P.tile_vstart[t];
+    for (int g = P.tile_gstart[t]; g < P.tile_gstart[t + 1]; ++g)
+      for (int e = P.group_estart[g]; e < P.group_estart[g + 1]; ++e) {
+        const int eu = P.elem_user[e];
+        if (tile_of_cell) tile_of_cell[eu] = t;
+        if (group_of_cell) group_of_cell[eu] = g;
+        if (slot_cells)
+          for (int a = 0; a < 4; ++a)
+            slot_cells[4 * (size_t)eu + a] = uoi[P.tv_vid[vs + (int)((P.ids[e] >> (8 * a)) & 0xffu)]];
+      }
+  }
+  return AGB_OK;
+}
+
 int agb_fem_cells(const agb_fem* f, int32_t* cells_out, uint32_t* tile_color_hash) {
   AGB_REQUIRE(f && cells_out, AGB_E_INVALID, "agb_fem_cells: null argument");
   const TilePlan& P = f->plan;

@@ -106,10 +106,23 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
 int agb_fem_destroy(agb_fem* fem);
 /* tile statistics: n_tiles, n_tile_vertices (host out; any may be NULL) */
 int agb_fem_info(const agb_fem* fem, int32_t* n_tiles, int32_t* n_tile_vertices);
+/* Host only (no device work): the tile and warp-group plan that a potential
+ * over these cells builds -- vertices in Morton order of `points`, elements
+ * in Morton order of their centroids, tiles of <= tile_elems (0: 1024)
+ * elements and <= 256 vertices, warp groups of <= 32 elements in which every
+ * corner slot holds 32 distinct vertices (the colouring that lets a warp
+ * accumulate without atomics).  Outputs per caller cell (may be NULL): its
+ * tile, its group, and its four corners in stored slot order (caller point
+ * ids).  For inspection and tests of the plan. */
+int agb_plan_tiles(int32_t n_points, int32_t n_cells, const int32_t* cells, const double* points,
+                   int32_t tile_elems, int32_t* n_tiles, int32_t* n_groups, int32_t* tile_of_cell,
+                   int32_t* group_of_cell, int32_t* slot_cells);
+
 /* Connectivity as stored after the Morton reorder, tiling and warp-group
  * colouring: cells_out[4 c + a] = caller point id of stored corner a of the
- * caller's cell c (corners of a cell may be permuted by the colouring; the
- * set and the orientation are kept).  tile_color_hash (may be NULL) receives a
+ * caller's cell c (the colouring permutes a cell's corners, with the element
+ * gradients permuted alike; the corner set is kept, the orientation of the
+ * stored order may be odd).  tile_color_hash (may be NULL) receives a
  * hash of the whole tile / group / corner-slot plan, for bit-exactness checks
  * across builds and machines.  Host only; no reference counterpart. */
 int agb_fem_cells(const agb_fem* fem, int32_t* cells_out, uint32_t* tile_color_hash);
