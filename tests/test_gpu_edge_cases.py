@@ -183,3 +183,33 @@ def test_argument_checks(cuda_device):
     with pytest.raises(TypeError):
         pot.fun(torch.zeros((4, 3), dtype=torch.float32, device=cuda_device),
                 torch.zeros(1, dtype=torch.float32, device=cuda_device))
+
+
+def _tet_displacement_for(F):
+    """u with deformation gradient F on TET (u_a = (F - I) X_a)."""
+    return (TET - TET[0]) @ (np.asarray(F) - np.eye(3)).T
+
+
+@pytest.mark.parametrize("case", ["inverted", "rotation", "repeated_singular_values", "near_flat"])
+def test_arap_svd_edge_cases_fp64(case, cuda_device):
+    """ARAP at deformation gradients where the 3x3 SVD is delicate: an
+    inverted tet (rotation-variant convention, det R = +1), a pure rotation
+    (zero energy and force), repeated singular values (R unique although U
+    and V are not), and a nearly flat tet."""
+    cells = np.array([[0, 1, 2, 3]], np.int32)
+    c, s_ = np.cos(0.7), np.sin(0.7)
+    Rz = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
+    F = {"inverted": np.diag([1.1, 0.9, -0.8]) @ Rz,
+         "rotation": Rz,
+         "repeated_singular_values": Rz @ np.diag([1.2, 1.2, 0.9]),
+         "near_flat": np.diag([1.0, 1.0, 1e-3]) @ Rz}[case]
+    u = _tet_displacement_for(F)
+    p = np.random.default_rng(6).normal(size=(4, 3))
+    ora = O.FemPotential.from_mesh(O.Material.ARAP, TET, cells, mu=2.0)
+    pot = ag.Arap(cells, 2.0, points=TET, dtype=torch.float64)
+    got = _eval_all(pot, u, p, cuda_device)
+    ref = _ora_all(ora, u, p)
+    if case == "rotation":
+        assert abs(float(got["fun"][0])) < 1e-12 and np.abs(got["grad"]).max() < 1e-12
+        return
+    _check(got, ref, 1e-9)
