@@ -672,7 +672,7 @@ int agb_solver_destroy(agb_solver* sv) {
                   (void*)sv->d_group_estart, (void*)sv->d_tv_vid,
                   (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_xa, sv->d_gd, sv->d_p0,
                   sv->d_p1, sv->d_xref, sv->d_gref, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
-                  sv->d_u_tmp})
+                  sv->d_u_tmp, sv->d_act})
     dfree(p);
   if (sv->h_state) cudaFreeHost(sv->h_state);
   delete sv;
@@ -683,12 +683,17 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   AGB_REQUIRE(out && m, AGB_E_INVALID, "agb_solver_create: null argument");
   *out = nullptr;
   AGB_REQUIRE(!m->fems.empty(), AGB_E_INVALID, "agb_solver_create: the model has no FEM potential");
-  const int mat = m->fems[0]->material;
-  for (agb_fem* f : m->fems)
-    AGB_REQUIRE(f->material == mat, AGB_E_INVALID,
-                "agb_solver_create: potentials of one solver must share a material");
-  AGB_REQUIRE(mat != AGB_STABLE_NEO_HOOKEAN_MUSCLE || m->fems.size() == 1, AGB_E_INVALID,
-              "agb_solver_create: a muscle model has one potential (its activation records are used in place)");
+  // one material per solver; stable Neo-Hookean and muscle potentials mix as
+  // muscles (a stable Neo-Hookean cell is a muscle cell with zero activation)
+  bool any_arap = false, any_snh = false, any_muscle = false;
+  for (agb_fem* f : m->fems) {
+    any_arap |= f->material == AGB_ARAP;
+    any_snh |= f->material == AGB_STABLE_NEO_HOOKEAN;
+    any_muscle |= f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+  }
+  AGB_REQUIRE(!(any_arap && (any_snh || any_muscle)), AGB_E_INVALID,
+              "agb_solver_create: ARAP and stable Neo-Hookean potentials cannot share a solver");
+  const int mat = any_arap ? AGB_ARAP : (any_muscle ? AGB_STABLE_NEO_HOOKEAN_MUSCLE : AGB_STABLE_NEO_HOOKEAN);
   agb_pncg_params prm;
   agb_pncg_default_params(&prm);
   if (params) prm = *params;
@@ -734,14 +739,22 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
     }
     P.group_estart.push_back(P.n_cells);
     P.D.assign(9 * (size_t)P.n_cells, 0.0);
+    // muscle solvers: records hold D A (D for stable Neo-Hookean potentials)
+    // and the activation stream is concatenated (zeros for them)
+    std::vector<double> act_all;
+    if (mat == AGB_STABLE_NEO_HOOKEAN_MUSCLE) act_all.assign(6 * (size_t)P.n_cells, 0.0);
     int eoff = 0;
     for (agb_fem* f : m->fems) {
       const TilePlan& Q = f->plan;
+      const bool muscle = f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+      const std::vector<double> DA = muscle ? muscle_D(Q, f->act_internal) : std::vector<double>();
+      const std::vector<double>& Dq = muscle ? DA : Q.D;
       for (int k = 0; k < 9; ++k)
-        std::memcpy(&P.D[(size_t)k * P.n_cells + eoff], &Q.D[(size_t)k * Q.n_cells],
-                    sizeof(double) * Q.n_cells);
+        std::memcpy(&P.D[(size_t)k * P.n_cells + eoff], &Dq[(size_t)k * Q.n_cells], sizeof(double) * Q.n_cells);
+      if (muscle) std::memcpy(&act_all[6 * (size_t)eoff], f->act_internal.data(), sizeof(double) * 6 * Q.n_cells);
       eoff += Q.n_cells;
     }
+    if (!rc && !act_all.empty()) rc = upload_act(act_all, (size_t)P.n_cells, sv->precision, &sv->d_act);
     if (!rc) rc = dupload(&sv->d_tile_estart, P.tile_estart);
     if (!rc) rc = dupload(&sv->d_tile_vstart, P.tile_vstart);
     if (!rc) rc = dupload(&sv->d_tile_gstart, P.tile_gstart);
@@ -758,6 +771,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
     sv->fv.tv_vid = sv->d_tv_vid;
     sv->fv.rec = sv->d_rec;
     sv->fv.ids = sv->d_ids;
+    sv->fv.act = sv->d_act;
   }
   if (!rc) rc = dupload(&sv->d_slot_of_tv, slot_of_tv);
   const size_t v4 = v4_bytes(sv->precision);

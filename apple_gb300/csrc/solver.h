@@ -228,6 +228,7 @@ struct agb_solver {
   unsigned* d_cnt = nullptr;
   agb::SolverState* d_state = nullptr;
   agb::SolverState* h_state = nullptr;  // pinned
+  void* d_act = nullptr;                // several potentials: concatenated activation stream (muscle)
   void* d_u_tmp = nullptr;              // caller-order staging for host I/O
   agb::SolveArgs args{};
   // adjoint CG (allocated on first use)

@@ -245,3 +245,60 @@ def test_activation_gradient_fp64_vs_oracle_and_central_difference(cuda_device):
             vals.append(float(loss_of(prob.solve(torch.tensor(mu), torch.tensor(lam), torch.tensor(a2)))))
         fd = (vals[0] - vals[1]) / (2 * h)
         assert da[c, k] == pytest.approx(fd, rel=1e-4, abs=1e-9 * np.abs(da).max())
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_passive_and_muscle_regions_in_one_solve(dtype, cuda_device):
+    """A column whose lower half is passive stable Neo-Hookean and whose upper
+    half is an activated muscle: two potentials over one vertex set, solved
+    by one device PNCG (the passive cells run as muscle cells with zero
+    activation) against the oracle's two-potential model."""
+    m = meshgen.grid(4, 4, 8)
+    lam, mu = meshgen.lame_converter(1e4, 0.45)
+    zc = m.points[m.cells].mean(1)[:, 2]
+    upper = zc > 0.5 * m.points[:, 2].max()
+    act = np.zeros((int(upper.sum()), 6))
+    act[:, 2] = -0.15
+    act[:, 0] = act[:, 1] = 0.075
+    mask = np.zeros((m.n_points, 3), bool)
+    mask[meshgen.face_mask(m, 2, "min")] = True
+    fv = np.zeros((m.n_points, 3))
+    force = meshgen.lumped_gravity(m, 100.0)
+
+    def part(sel, muscle):
+        mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells[sel]), mu, lam)
+        if muscle:
+            mesh.cell_data["activation"] = act
+        return mesh
+
+    full = meshgen.TetMesh(m.points, m.cells)
+    full.point_data["FixedMask"] = mask
+    full.point_data["FixedValue"] = fv
+    b = ag.ModelBuilder(dtype=dtype)
+    b.add_vertices(full)
+    b.add_fixed(full)
+    b.add_potential(ag.StableNeoHookean.from_pyvista(part(~upper, False), dtype=dtype))
+    b.add_potential(ag.StableNeoHookeanMuscle.from_pyvista(part(upper, True), dtype=dtype))
+    fmesh = meshgen.TetMesh(m.points, m.cells)
+    fmesh.point_data["Force"] = force
+    fmesh.point_data["GlobalPointId"] = np.arange(m.n_points)
+    b.add_potential(ag.ExternalForce.from_pyvista(fmesh, dtype=dtype))
+    model = b.finalize()
+    passive = O.FemPotential.from_mesh(O.Material.STABLE_NEO_HOOKEAN, m.points, m.cells[~upper], mu=mu, lam=lam)
+    muscle = O.FemPotential.from_mesh(O.Material.STABLE_NEO_HOOKEAN_MUSCLE, m.points, m.cells[upper], mu=mu,
+                                      lam=lam, activation=act)
+    om = O.Model(O.DofMap(m.n_points, mask, fv), [passive, muscle], O.ExternalForce(np.arange(m.n_points), force))
+    u_ref, _ = O.solve_model(om, rtol=1e-9, max_steps=5000)
+    rtol = 1e-8 if dtype == torch.float64 else 1e-6
+    fwd = ag.Forward(model, ag.PNCG(ag.ConvergenceCriteria(max_steps=5000, rtol=rtol)))
+    sol = fwd.step()
+    assert sol.result == ag.Result.PRIMARY_SUCCESS, sol
+    fwd_u = fwd.state.u.double().cpu().numpy()
+    diag = np.linalg.norm(m.points.max(0) - m.points.min(0))
+    assert np.abs(fwd_u - u_ref).max() < 1e-5 * diag
+    # the model's own evaluation (per-potential kernels) agrees with the oracle too
+    U = torch.tensor(u_ref, dtype=dtype, device=cuda_device)
+    g = model.grad(U).double().cpu().numpy()
+    g_ref = om.grad(u_ref)
+    free = ~mask
+    assert np.linalg.norm((g - g_ref)[free]) <= (1e-9 if dtype == torch.float64 else 1e-4) * np.linalg.norm(force)
