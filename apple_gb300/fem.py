@@ -327,8 +327,10 @@ class StableNeoHookeanMuscle(WarpPotentialFem):
         return h
 
     def set_activation(self, activation) -> None:
-        """Replace the per-cell activation on every device copy of this potential
-        (solvers built on it see the new records at their next launch)."""
+        """Replace the per-cell activation on every device copy of this potential.
+        A solver whose model has this as its only FEM potential sees the new
+        records at its next launch; a solver over several potentials copied
+        the records when it was created and needs to be built again."""
         self.activation = _activation_array(activation, self.cells.shape[0])
         handles = list(self._by_space.values()) + ([self._own[1]] if self._own is not None else [])
         for h in handles:
