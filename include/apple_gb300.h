@@ -218,6 +218,11 @@ typedef struct agb_pncg_stats {
 
 void agb_pncg_default_params(agb_pncg_params* params);
 
+/* A PNCG solver over the model (Forward.step / Optimizer.minimize,
+ * forward/_forward.py:52-56).  The model's FEM potentials must be all ARAP, or
+ * all stable Neo-Hookean and muscle (mixed ones run as muscle cells, the
+ * stable Neo-Hookean ones with zero activation).  A single FEM potential's
+ * element records are used in place; several are copied and concatenated. */
 int agb_solver_create(agb_model* model, const agb_pncg_params* params, agb_solver** out);
 int agb_solver_destroy(agb_solver* solver);
 /* load u (device, full vector; fixed components are overwritten by the
