@@ -5,8 +5,9 @@ Workload: 50 x 50 x 120 cubes of side 1/50 split 5 tets per cube
 (1,500,000 tets, 314,721 vertices), E = 1e5, nu = 0.49, z = 0 face fixed,
 z = max face displaced +30% of the length along z, FP32 element arithmetic
 with float-float/FP64 reductions.  A step is one PNCG iteration (direction
-pass, gradient pass, vertex pass: one CUDA graph launch); the PNCG state
-carries across steps.  L2 is flushed (256 MiB device write) before every
+pass, gradient pass, vertex pass, and the two reference-state refresh passes
+that return at once unless a refresh is due: one CUDA graph launch); the PNCG
+state carries across steps.  L2 is flushed (256 MiB device write) before every
 timed step; each step is timed with CUDA events on the launching stream.
 
 Also reported: the dominant pass timed alone against the measured HBM peak
@@ -17,6 +18,12 @@ path on this host's cores).
 
 ``--impl reference`` times that CPU restatement on the same workload.
 Multi-GPU (torchrun): independent replicas, one per rank (weak scaling).
+
+Other workloads (``--config``): ``grid64`` (64x64x96 cells, ARAP and stable
+Neo-Hookean, FP32 and FP64), ``irregular`` (Delaunay ball), ``batched`` (512
+uneven grids in one batch vs one by one), ``adjoint`` (138k-tet material
+gradient vs finite differences), ``muscle`` (the headline grid as an activated
+muscle) and ``hbm-sizes`` (cold bandwidth vs bytes per launch).
 """
 
 from __future__ import annotations
