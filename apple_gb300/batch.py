@@ -24,9 +24,11 @@ from .pncg import PNCG, Result, Solution
 
 
 class BatchedForward:
-    """``models``: :class:`apple_gb300.model.Model` objects (stable Neo-Hookean
-    potentials of one dtype). ``solve()`` minimises every model's energy from
-    its current state (zero free displacement, fixed values applied)."""
+    """``models``: :class:`apple_gb300.model.Model` objects of one dtype with
+    stable Neo-Hookean or muscle potentials (with any muscle in the batch,
+    every cell runs as a muscle cell, the plain ones with zero activation).
+    ``solve()`` minimises every model's energy from its current state (zero
+    free displacement, fixed values applied)."""
 
     def __init__(self, models, optimizer: PNCG | None = None, *, chunk_verts: int = 0):
         if not models:

@@ -26,7 +26,7 @@ namespace {
 
 constexpr int kTailThreads = 256;
 
-template <class R>
+template <class R, int MAT>
 __global__ void __launch_bounds__(kElemThreads) batch_dir_kernel(BatchArgs b) {
   constexpr int N = 6;
   constexpr unsigned FF = 0x2u;  // float-float warp tree for c2 (terms of both signs)
@@ -50,10 +50,11 @@ __global__ void __launch_bounds__(kElemThreads) batch_dir_kernel(BatchArgs b) {
   for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
     ElemGeo<R> geo;
     uint32_t ids;
-    load_elem<R>(a.fv, e, geo, ids);
+    load_elem_m<R, MAT>(a.fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
     R G[3][3], dF[3][3];
     vec_gradient(sx, l, geo.D, G);
+    add_act<MAT>(geo, G);
     vec_gradient(sp, l, geo.D, dF);
     SnhPoint<R> s;
     snh_prepare(G, s);
@@ -96,9 +97,9 @@ __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs 
   }
 }
 
-template <class R, bool DELTA>
+template <class R, int MAT, bool DELTA>
 __global__ void __launch_bounds__(kGradThreads, 6) batch_grad_kernel(BatchArgs b) {
-  grad_tile<R, AGB_STABLE_NEO_HOOKEAN, DELTA>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
+  grad_tile<R, MAT, DELTA>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
 }
 
 template <class R, bool DELTA>
@@ -173,12 +174,13 @@ __global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchAr
 
 // reference-state refresh of the models that asked for one (FP32)
 // (grid-stride over tiles / chunks with a resident-sized grid)
+template <int MAT>
 __global__ void __launch_bounds__(kGradThreads) batch_ref_elem_kernel(BatchArgs b) {
   pdl_trigger();
   pdl_wait();
   for (int tile = blockIdx.x; tile < b.a.fv.n_tiles; tile += gridDim.x) {
     if (!b.st[b.tile_mesh[tile]].refresh) continue;  // uniform across the CTA
-    ref_tile<AGB_STABLE_NEO_HOOKEAN>(b.a, tile);
+    ref_tile<MAT>(b.a, tile);
     __syncthreads();
   }
 }
@@ -196,9 +198,9 @@ __global__ void batch_force_refresh_kernel(BatchArgs b) {
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < b.n_meshes; m += gridDim.x * blockDim.x) b.st[m].refresh = 1;
 }
 
-template <class R>
+template <class R, int MAT>
 __global__ void __launch_bounds__(kElemThreads) batch_energy_pass_kernel(BatchArgs b) {
-  energy_tile<R, AGB_STABLE_NEO_HOOKEAN>(b.a, blockIdx.x, (AccStore<R>*)b.part_grad + blockIdx.x);
+  energy_tile<R, MAT>(b.a, blockIdx.x, (AccStore<R>*)b.part_grad + blockIdx.x);
 }
 
 template <class R>
@@ -275,16 +277,19 @@ cudaError_t launch_pdl_b(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cu
 }
 
 cudaError_t batch_refresh(const BatchArgs& b, cudaStream_t s) {
-  cudaError_t e = launch_pdl_b(batch_ref_elem_kernel, dim3(ref_blocks(b.a.fv.n_tiles)), dim3(kGradThreads),
-                               ref_smem_bytes(), s, b);
+  cudaError_t e = b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
+                      ? launch_pdl_b(batch_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN_MUSCLE>,
+                                     dim3(ref_blocks(b.a.fv.n_tiles)), dim3(kGradThreads), ref_smem_bytes(), s, b)
+                      : launch_pdl_b(batch_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN>, dim3(ref_blocks(b.a.fv.n_tiles)),
+                                     dim3(kGradThreads), ref_smem_bytes(), s, b);
   const int vb = b.n_chunks < kSMs * 8 ? b.n_chunks : kSMs * 8;
   if (e == cudaSuccess) e = launch_pdl_b(batch_ref_vertex_kernel, dim3(vb > 0 ? vb : 1), dim3(kVThreads), 0, s, b);
   return e;
 }
 
-template <class R, bool DELTA>
+template <class R, int MAT, bool DELTA>
 cudaError_t batch_grad_and_vertex_d(const BatchArgs& b, cudaStream_t s) {
-  cudaError_t e = launch_pdl_b(batch_grad_kernel<R, DELTA>, dim3(b.a.fv.n_tiles), dim3(kGradThreads),
+  cudaError_t e = launch_pdl_b(batch_grad_kernel<R, MAT, DELTA>, dim3(b.a.fv.n_tiles), dim3(kGradThreads),
                                grad_smem_bytes<R>(), s, b);
   if (e == cudaSuccess) e = launch_pdl_b(batch_vertex_kernel<R, DELTA>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
   if (e == cudaSuccess)
@@ -293,30 +298,46 @@ cudaError_t batch_grad_and_vertex_d(const BatchArgs& b, cudaStream_t s) {
   return e;
 }
 
+template <class R, int MAT>
+cudaError_t batch_grad_and_vertex_m(const BatchArgs& b, cudaStream_t s) {
+  if (b.a.delta) {
+    if (!kRefDelta<R, MAT> || !b.a.xref || !b.a.gref) return cudaErrorInvalidValue;
+    return batch_grad_and_vertex_d<R, MAT, kRefDelta<R, MAT>>(b, s);
+  }
+  return batch_grad_and_vertex_d<R, MAT, false>(b, s);
+}
+
 template <class R>
 cudaError_t batch_grad_and_vertex(const BatchArgs& b, cudaStream_t s) {
-  if (b.a.delta) {
-    if (!kRefDelta<R, AGB_STABLE_NEO_HOOKEAN> || !b.a.xref || !b.a.gref) return cudaErrorInvalidValue;
-    return batch_grad_and_vertex_d<R, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>(b, s);
-  }
-  return batch_grad_and_vertex_d<R, false>(b, s);
+  return b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
+             ? batch_grad_and_vertex_m<R, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(b, s)
+             : batch_grad_and_vertex_m<R, AGB_STABLE_NEO_HOOKEAN>(b, s);
+}
+
+template <class R, int MAT>
+cudaError_t batch_iteration_m(const BatchArgs& b, cudaStream_t s) {
+  batch_dir_kernel<R, MAT><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_pdl_b(batch_dir_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  if (e == cudaSuccess) e = batch_grad_and_vertex_m<R, MAT>(b, s);
+  return e;
 }
 
 template <class R>
 cudaError_t batch_iteration_t(const BatchArgs& b, cudaStream_t s) {
-  batch_dir_kernel<R><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = launch_pdl_b(batch_dir_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
-  if (e == cudaSuccess) e = batch_grad_and_vertex<R>(b, s);
-  return e;
+  return b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE ? batch_iteration_m<R, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(b, s)
+                                                          : batch_iteration_m<R, AGB_STABLE_NEO_HOOKEAN>(b, s);
 }
 
 template <class R>
 cudaError_t batch_prepare_t() {
   const cudaFuncAttribute m = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t e = cudaFuncSetAttribute(batch_grad_kernel<R, false>, m, (int)grad_smem_bytes<R>());
-  if (e == cudaSuccess && kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>)
-    e = cudaFuncSetAttribute(batch_grad_kernel<R, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>, m, (int)grad_smem_bytes<R>());
+  const int g = (int)grad_smem_bytes<R>();
+  constexpr int SNH = AGB_STABLE_NEO_HOOKEAN, MU = AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+  cudaError_t e = cudaFuncSetAttribute(batch_grad_kernel<R, SNH, false>, m, g);
+  if (e == cudaSuccess && kRefDelta<R, SNH>) e = cudaFuncSetAttribute(batch_grad_kernel<R, SNH, kRefDelta<R, SNH>>, m, g);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_grad_kernel<R, MU, false>, m, g);
+  if (e == cudaSuccess && kRefDelta<R, MU>) e = cudaFuncSetAttribute(batch_grad_kernel<R, MU, kRefDelta<R, MU>>, m, g);
   return e;
 }
 
@@ -363,11 +384,18 @@ cudaError_t launch_batch_set_limit(const BatchArgs& b, int n, cudaStream_t s) {
 
 cudaError_t launch_batch_energy(const BatchArgs& b, cudaStream_t s) {
   if (b.n_meshes == 0) return cudaSuccess;
+  const bool mu = b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
   if (b.a.precision == AGB_F64) {
-    batch_energy_pass_kernel<double><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+    if (mu)
+      batch_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+    else
+      batch_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     batch_energy_kernel<double><<<b.n_meshes, kTailThreads, 0, s>>>(b);
   } else {
-    batch_energy_pass_kernel<float><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+    if (mu)
+      batch_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+    else
+      batch_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     batch_energy_kernel<float><<<b.n_meshes, kTailThreads, 0, s>>>(b);
   }
   return cudaGetLastError();

@@ -1226,7 +1226,7 @@ int agb_batch_destroy(agb_batch* b) {
                   (void*)b->d_slot_of_tv, (void*)b->d_off, (void*)b->d_uoi, b->d_fixed, b->d_force,
                   (void*)b->d_tile_mesh, (void*)b->d_mesh_tile0, (void*)b->d_chunk_v0, (void*)b->d_chunk_mesh,
                   (void*)b->d_mesh_chunk0, b->d_xa, b->d_gd, b->d_p0, b->d_p1, b->d_xref, b->d_gref, b->d_slots,
-                  b->d_part,
+                  b->d_part, b->d_act,
                   (void*)b->d_state, (void*)b->d_bstate})
     dfree(p);
   if (b->h_state) cudaFreeHost(b->h_state);
@@ -1244,9 +1244,15 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
     AGB_REQUIRE(m && !m->fems.empty(), AGB_E_INVALID, "agb_batch_create: model %d has no FEM potential", k);
     AGB_REQUIRE(m->precision == prec, AGB_E_INVALID, "agb_batch_create: models must share a precision");
     for (agb_fem* f : m->fems)
-      AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN, AGB_E_INVALID,
-                  "agb_batch_create: the batched form runs stable Neo-Hookean potentials");
+      AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN || f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE,
+                  AGB_E_INVALID, "agb_batch_create: the batched form runs stable Neo-Hookean and muscle potentials");
   }
+  // with any muscle potential every cell runs as a muscle cell (zero activation
+  // for the stable Neo-Hookean ones)
+  bool any_muscle = false;
+  for (int k = 0; k < n_models; ++k)
+    for (agb_fem* f : models[k]->fems) any_muscle |= f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+  const int bmat = any_muscle ? AGB_STABLE_NEO_HOOKEAN_MUSCLE : AGB_STABLE_NEO_HOOKEAN;
   agb_pncg_params prm;
   agb_pncg_default_params(&prm);
   if (params) prm = *params;
@@ -1313,13 +1319,19 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   }
   P.group_estart.push_back(P.n_cells);
   P.D.assign(9 * (size_t)P.n_cells, 0.0);
+  std::vector<double> act_all;
+  if (any_muscle) act_all.assign(6 * (size_t)P.n_cells, 0.0);
   {
     size_t eoff = 0;
     for (agb_model* m : b->models)
       for (agb_fem* f : m->fems) {
         const TilePlan& Q = f->plan;
+        const bool muscle = f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+        const std::vector<double> DA = muscle ? muscle_D(Q, f->act_internal) : std::vector<double>();
+        const std::vector<double>& Dq = muscle ? DA : Q.D;
         for (int c = 0; c < 9; ++c)
-          std::memcpy(&P.D[(size_t)c * P.n_cells + eoff], &Q.D[(size_t)c * Q.n_cells], sizeof(double) * Q.n_cells);
+          std::memcpy(&P.D[(size_t)c * P.n_cells + eoff], &Dq[(size_t)c * Q.n_cells], sizeof(double) * Q.n_cells);
+        if (muscle) std::memcpy(&act_all[6 * eoff], f->act_internal.data(), sizeof(double) * 6 * Q.n_cells);
         eoff += Q.n_cells;
       }
   }
@@ -1333,6 +1345,7 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   if (!rc) rc = dupload(&b->d_group_estart, P.group_estart);
   if (!rc) rc = dupload(&b->d_tv_vid, P.tv_vid);
   if (!rc) rc = upload_records(P, prec, &b->d_rec, &b->d_ids);
+  if (!rc && any_muscle) rc = upload_act(act_all, (size_t)P.n_cells, prec, &b->d_act);
   if (!rc) rc = dupload(&b->d_slot_of_tv, slot_of_tv);
   if (!rc) rc = dupload(&b->d_off, off);
   if (!rc) rc = dupload(&b->d_uoi, uoi);
@@ -1384,7 +1397,8 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   }
   BatchArgs& ba = b->args;
   SolveArgs& a = ba.a;
-  a.fv.material = AGB_STABLE_NEO_HOOKEAN;
+  a.fv.material = bmat;
+  a.fv.act = b->d_act;
   a.fv.n_tiles = P.n_tiles;
   a.fv.n_cells = P.n_cells;
   a.fv.tile_estart = b->d_tile_estart;

@@ -260,6 +260,7 @@ struct agb_batch {
   int32_t* d_tile_gstart = nullptr;
   int32_t* d_group_estart = nullptr;
   int32_t* d_tv_vid = nullptr;
+  void* d_act = nullptr;           // muscle activation stream (any muscle potential), else null
   void* d_rec = nullptr;
   uint32_t* d_ids = nullptr;
   int32_t* d_slot_of_tv = nullptr;

@@ -95,3 +95,44 @@ def test_autotuner_picks_a_candidate(cuda_device):
                    tile_elems=(256, 1024), chunk_verts=(256, 512), iters=3)
     assert (res.tile_elems, res.chunk_verts) in [(t, c) for t, c, _ in res.table]
     assert res.ms_per_iter == min(ms for _, _, ms in res.table)
+
+
+def _muscle_model(m, f, dtype, act):
+    mm = meshgen.TetMesh(m.points, m.cells)
+    mm.cell_data.update(m.cell_data)
+    mm.point_data.update(m.point_data)
+    mm.cell_data["activation"] = act
+    b = ag.ModelBuilder(dtype=dtype)
+    b.add_vertices(mm)
+    b.add_fixed(mm)
+    b.add_potential(ag.StableNeoHookeanMuscle.from_pyvista(mm, dtype=dtype))
+    fm = meshgen.TetMesh(m.points, m.cells)
+    fm.point_data["Force"] = f
+    fm.point_data["GlobalPointId"] = np.arange(m.n_points)
+    b.add_potential(ag.ExternalForce.from_pyvista(fm, dtype=dtype))
+    return b.finalize()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_batch_with_muscle_models(cuda_device, dtype):
+    """Stable Neo-Hookean and activated muscle models in one batch (all cells
+    run as muscle cells, the plain ones with zero activation): each model
+    follows its own plain solve."""
+    cases = _cases(5, seed=3)
+    rng = np.random.default_rng(4)
+    acts = {1: 0.05 * rng.normal(size=(cases[1][0].n_cells, 6)), 3: 0.05 * rng.normal(size=(cases[3][0].n_cells, 6))}
+    rtol = 1e-10 if dtype == torch.float64 else 1e-6
+    crit = ag.ConvergenceCriteria(max_steps=20000, rtol=rtol)
+
+    def build(k):
+        m, f = cases[k]
+        return _muscle_model(m, f, dtype, acts[k]) if k in acts else _model(m, f, dtype)
+
+    bf = BatchedForward([build(k) for k in range(len(cases))], ag.PNCG(crit))
+    sols, us = bf.solve()
+    bar = 1e-7 if dtype == torch.float64 else 1e-5
+    for k, (sol, u) in enumerate(zip(sols, us)):
+        assert sol.result == ag.Result.PRIMARY_SUCCESS, (k, sol)
+        fwd = ag.Forward(build(k), ag.PNCG(crit))
+        assert fwd.step().result == ag.Result.PRIMARY_SUCCESS
+        assert float((u.double() - fwd.state.u.double()).abs().max()) < bar * _diag(cases[k][0]), k
