@@ -4,8 +4,8 @@ Host side in Python (this package) over hand-written sm_103a CUDA kernels in
 ``libapple_gb300.so`` (C ABI: ``include/apple_gb300.h``).
 """
 
-from . import meshgen, vtu
-from .fem import Arap, Space, StableNeoHookean, StableNeoHookeanMuscle, WarpPotentialFem, with_lame
+from . import meshgen, vtu, warp
+from .fem import Arap, Space, StableNeoHookean, StableNeoHookeanMuscle, WarpPotential, WarpPotentialFem, with_lame
 from .forward import Forward, ForwardProblem, ModelState
 from .model import DofMap, DofMapBuilder, Model, ModelBuilder, WarpModel
 from .pncg import PNCG, ConvergenceCriteria, LineSearch, Result, Solution
@@ -32,8 +32,10 @@ __all__ = [
     "StableNeoHookean",
     "StableNeoHookeanMuscle",
     "WarpModel",
+    "WarpPotential",
     "WarpPotentialFem",
     "meshgen",
     "vtu",
+    "warp",
     "with_lame",
 ]

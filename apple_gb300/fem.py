@@ -84,7 +84,28 @@ class Space:
             self.handle = None
 
 
-class WarpPotentialFem:
+class WarpPotential:
+    """The energy-term interface of warp/model/_potential.py:9-32: every
+    method accumulates into ``output`` (the caller zeroes it); the base
+    raises ``NotImplementedError`` like the reference's."""
+
+    def fun(self, u: torch.Tensor, output: torch.Tensor) -> None:
+        raise NotImplementedError
+
+    def grad(self, u: torch.Tensor, output: torch.Tensor) -> None:
+        raise NotImplementedError
+
+    def hess_diag(self, u: torch.Tensor, output: torch.Tensor) -> None:
+        raise NotImplementedError
+
+    def hess_prod(self, u: torch.Tensor, p: torch.Tensor, output: torch.Tensor) -> None:
+        raise NotImplementedError
+
+    def hess_quad(self, u: torch.Tensor, p: torch.Tensor, output: torch.Tensor) -> None:
+        raise NotImplementedError
+
+
+class WarpPotentialFem(WarpPotential):
     """A tetrahedral FEM energy term on the GPU."""
 
     material: int = -1

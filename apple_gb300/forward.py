@@ -7,8 +7,11 @@ import functools
 
 import torch
 
-from .model import Model
+from .model import DofMap, DofMapBuilder, Model, ModelBuilder
 from .pncg import PNCG, ConvergenceCriteria, LineSearch, Solution
+
+# the names of liblaf.apple.forward (forward/__init__.pyi)
+__all__ = ["DofMap", "DofMapBuilder", "Forward", "ForwardProblem", "Model", "ModelBuilder", "ModelState"]
 
 
 @dataclasses.dataclass

@@ -13,11 +13,11 @@ import numpy as np
 import torch
 
 from . import _lib
-from .fem import Space, _default_name, check_scalar, check_vec, dtype_code, ptr, stream_ptr
+from .fem import Space, WarpPotential, _default_name, check_scalar, check_vec, dtype_code, ptr, stream_ptr
 from .region import FORCE, GLOBAL_POINT_ID, mesh_points, point_data
 
 
-class ExternalForce:
+class ExternalForce(WarpPotential):
     def __init__(self, indices, force, *, n_points: int | None = None, name: str | None = None,
                  dtype: torch.dtype = torch.float32):
         self.indices = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1)
