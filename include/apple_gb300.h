@@ -128,8 +128,11 @@ int agb_plan_tiles(int32_t n_points, int32_t n_cells, const int32_t* cells, cons
 int agb_fem_cells(const agb_fem* fem, int32_t* cells_out, uint32_t* tile_color_hash);
 /* Muscle potentials: set the per-cell activation a (host, n_cells x 6, the
  * caller's cell order; cell data `activation`, common/attr_name.py:40-44,
- * utils/_material.py:15-16).  The element records are rebuilt in place, so a
- * solver over this single potential sees the new activation. */
+ * utils/_material.py:15-16).  The element records are rebuilt in place
+ * (synchronous copies on the default stream), so a solver whose model has this
+ * as its only FEM potential sees the new activation at its next launch; a
+ * solver over several potentials copied the records at creation.  Call it
+ * while no launch that reads this potential is in flight. */
 int agb_fem_set_activation(agb_fem* fem, const double* activation);
 
 /* WarpPotential methods (warp/fem/_base.py:151-194); accumulate into output.
