@@ -44,6 +44,7 @@ class PncgStats(ctypes.Structure):
         ("beta", c_double),
         ("line_search_steps", c_int32),
         ("line_search_ok", c_int32),
+        ("hess_diag_mean", c_double),
     ]
 
 
@@ -102,6 +103,7 @@ _SIGNATURES = {
     "agb_solver_iterate": (c_int, [c_void_p, c_int32, c_void_p]),
     "agb_solver_step": (c_int, [c_void_p, c_void_p]),
     "agb_solver_read": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
+    "agb_solver_read_direction": (c_int, [c_void_p, c_void_p, c_void_p]),
     "agb_pncg_minimize_host": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_solver_time_passes": (c_int, [c_void_p, c_int32, c_void_p, ctypes.c_size_t, POINTER(ctypes.c_float), c_void_p]),
     "agb_batch_create": (c_int, [c_int32, c_void_p, POINTER(PncgParams), c_int32, POINTER(c_void_p)]),

@@ -20,7 +20,7 @@ import torch
 
 from . import _lib
 from .fem import ptr, stream_ptr
-from .pncg import PNCG, Result, Solution
+from .pncg import PNCG, Solution
 
 
 class BatchedForward:
@@ -81,8 +81,7 @@ class BatchedForward:
         if with_u:
             u = torch.empty((int(self.offsets[-1]), 3), dtype=self.dtype, device="cuda")
         _lib.call("agb_batch_read", self.handle, ptr(u), ctypes.cast(st, ctypes.c_void_p), stream_ptr())
-        sols = [Solution(Result(s.result), s.n_steps, s.grad_norm, s.grad_norm_first, s.energy, s.alpha, s.beta,
-                         s.line_search_steps, bool(s.line_search_ok)) for s in st]
+        sols = [Solution.from_stats(s) for s in st]
         us = None if u is None else [u[self.offsets[k]:self.offsets[k + 1]] for k in range(n)]
         return sols, us
 

@@ -865,6 +865,7 @@ int agb_solver_reset(agb_solver* sv, const void* u, void* stream) {
     RC(check_launch(launch_solver_refresh(sv->args, s), "solver_refresh"));
   }
   RC(check_launch(launch_solver_first(sv->args, s), "solver_first"));
+  sv->has_state = true;
   return AGB_OK;
 }
 
@@ -947,6 +948,9 @@ int agb_solver_step(agb_solver* sv, void* stream) {
   return AGB_OK;
 }
 
+// the vertex pass stores the preconditioner's fill as its reciprocal
+static double hess_diag_mean(const SolverState& st) { return st.inv_mean > 0.0 ? 1.0 / st.inv_mean : 1.0; }
+
 int agb_solver_read(agb_solver* sv, void* u_out, agb_pncg_stats* stats, void* stream) {
   AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_read: null handle");
   cudaStream_t s = as_stream(stream);
@@ -969,8 +973,30 @@ int agb_solver_read(agb_solver* sv, void* u_out, agb_pncg_stats* stats, void* st
     stats->beta = st.beta;
     stats->line_search_steps = st.ls_steps;
     stats->line_search_ok = st.ls_ok;
+    stats->hess_diag_mean = hess_diag_mean(st);
   }
   AGB_REQUIRE(st.error == 0, AGB_E_DEVICE, "solver: device guard %d tripped", st.error);
+  return AGB_OK;
+}
+
+int agb_solver_read_direction(agb_solver* sv, void* p_host, void* stream) {
+  AGB_REQUIRE(sv && p_host, AGB_E_INVALID, "agb_solver_read_direction: null argument");
+  AGB_REQUIRE(sv->has_state, AGB_E_INVALID, "agb_solver_read_direction: call agb_solver_reset first");
+  cudaStream_t s = as_stream(stream);
+  AGB_CHECK_CUDA(cudaMemcpyAsync(sv->h_state, sv->d_state, sizeof(SolverState), cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  // the vertex pass flips pbuf after each iteration, so p[pbuf] (the next
+  // iteration's p_prev) holds the direction of the iteration just finished
+  const void* src = sv->h_state->pbuf ? sv->d_p1 : sv->d_p0;
+  const int np = sv->args.n_points;
+  const size_t rb = real_bytes(sv->precision);
+  std::vector<unsigned char> p4(4 * rb * (size_t)np);
+  AGB_CHECK_CUDA(cudaMemcpyAsync(p4.data(), src, p4.size(), cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  const std::vector<int32_t>& uoi = sv->model->space->user_of_internal;
+  unsigned char* out = static_cast<unsigned char*>(p_host);
+  for (int i = 0; i < np; ++i)  // V4 (x, y, z, pad) at internal i -> 3 reals at caller uoi[i]
+    std::memcpy(out + 3 * rb * (size_t)uoi[i], p4.data() + 4 * rb * (size_t)i, 3 * rb);
   return AGB_OK;
 }
 
@@ -1036,6 +1062,7 @@ int agb_solver_load(agb_solver* sv, const void* host, void* stream) {
     src += n;
   }
   AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  sv->has_state = true;
   return AGB_OK;
 }
 
@@ -1546,6 +1573,7 @@ int agb_batch_read(agb_batch* b, void* u_out, agb_pncg_stats* stats, void* strea
       stats[k].beta = st.beta;
       stats[k].line_search_steps = st.ls_steps;
       stats[k].line_search_ok = st.ls_ok;
+      stats[k].hess_diag_mean = hess_diag_mean(st);
     }
   }
   for (int k = 0; k < n; ++k)

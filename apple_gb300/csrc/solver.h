@@ -244,6 +244,7 @@ struct agb_solver {
   cudaGraphExec_t step_exec = nullptr;
   int step_kernels = 0;  // kernel nodes of one iteration
   cudaStream_t capture_stream = nullptr;
+  bool has_state = false;  // vertex state written (reset or checkpoint load)
 };
 
 struct agb_batch {

@@ -72,6 +72,12 @@ class Solution:
     beta: float
     line_search_steps: int
     line_search_ok: bool
+    hess_diag_mean: float = 1.0  # the preconditioner's fill for zero diagonal entries
+
+    @classmethod
+    def from_stats(cls, st: _lib.PncgStats) -> Solution:
+        return cls(Result(st.result), st.n_steps, st.grad_norm, st.grad_norm_first, st.energy, st.alpha, st.beta,
+                   st.line_search_steps, bool(st.line_search_ok), st.hess_diag_mean)
 
     @property
     def success(self) -> bool:
@@ -83,8 +89,23 @@ class Solution:
 
 
 @dataclasses.dataclass
+class HessDampingState:
+    """The fields the reference's progress logging reads from the optimizer
+    state (exp/2026/05/06/toy/src/20-ext-force-stable-neo-hookean-collision.py:
+    209,228-229).  This solver adds no damping to the Hessian, so ``factor``
+    is 0; ``hess_diag_mean`` is the mean of the positive free diagonal
+    entries, the preconditioner's fill for zero ones."""
+
+    factor: float
+    hess_diag_mean: float
+
+
+@dataclasses.dataclass
 class OptState:
-    """Per-iteration view for step-by-step driving (init/step/terminate)."""
+    """Per-iteration view for step-by-step driving (init/step/terminate).
+    ``direction`` is the last iteration's search direction over the free DOFs
+    (the step taken was ``line_search_state.alpha * direction``; zero after
+    init)."""
 
     n_steps: int
     line_search_state: LineSearchState
@@ -92,6 +113,8 @@ class OptState:
     beta: float
     done: bool
     result: Result
+    direction: torch.Tensor
+    hess_damping_state: HessDampingState
 
 
 @dataclasses.dataclass(frozen=True)
@@ -146,6 +169,13 @@ class DeviceSolver:
         blob = blob.to(dtype=torch.uint8, device="cpu").contiguous()
         _lib.call("agb_solver_load", self.handle, ctypes.c_void_p(blob.data_ptr()), stream_ptr())
 
+    def read_direction(self) -> torch.Tensor:
+        """The last iteration's search direction p (full (n_points, 3), CPU
+        tensor of the model dtype, zero on fixed DOFs and after reset)."""
+        p = torch.empty((self.warp_model.n_points, 3), dtype=self.warp_model.dtype)
+        _lib.call("agb_solver_read_direction", self.handle, ctypes.c_void_p(p.data_ptr()), stream_ptr())
+        return p
+
     def step_kernels(self) -> int:
         """Kernels one iteration launches (the nodes of the step graph)."""
         n = ctypes.c_int32()
@@ -155,8 +185,7 @@ class DeviceSolver:
     def read(self, u_out: torch.Tensor | None = None) -> Solution:
         st = _lib.PncgStats()
         _lib.call("agb_solver_read", self.handle, ptr(u_out), ctypes.byref(st), stream_ptr())
-        return Solution(Result(st.result), st.n_steps, st.grad_norm, st.grad_norm_first, st.energy, st.alpha,
-                        st.beta, st.line_search_steps, bool(st.line_search_ok))
+        return Solution.from_stats(st)
 
     def adjoint(self, rhs: torch.Tensor, *, rtol: float = 1e-6, atol: float = 0.0,
                 max_iter: int = 10000) -> tuple[torch.Tensor, "CgSolution"]:
@@ -177,8 +206,7 @@ class DeviceSolver:
         st = _lib.PncgStats()
         _lib.call("agb_pncg_minimize_host", self.handle, ctypes.c_void_p(u_host.data_ptr()), ctypes.byref(st),
                   stream_ptr())
-        return Solution(Result(st.result), st.n_steps, st.grad_norm, st.grad_norm_first, st.energy, st.alpha,
-                        st.beta, st.line_search_steps, bool(st.line_search_ok))
+        return Solution.from_stats(st)
 
 
 class PNCG:
@@ -233,14 +261,14 @@ class PNCG:
     def init(self, problem, state, free: torch.Tensor) -> OptState:
         sv = self.solver(problem)
         sv.reset(problem.before_trial(state, free).u)
-        return self._opt_state(sv)
+        return self._opt_state(problem, sv)
 
     def step(self, problem, state, opt_state: OptState):
         sv = self.solver(problem)
         sv.iterate(1)
         u_out = torch.empty_like(state.u)
         sv.read(u_out)
-        return dataclasses.replace(state, u=u_out), self._opt_state(sv, opt_state)
+        return dataclasses.replace(state, u=u_out), self._opt_state(problem, sv, opt_state)
 
     def terminate(self, problem, state, opt_state: OptState):
         return opt_state.done, opt_state.result
@@ -248,10 +276,12 @@ class PNCG:
     def postprocess(self, problem, state, opt_state: OptState, result) -> Solution:
         return self.solver(problem).read()
 
-    def _opt_state(self, sv: DeviceSolver, prev: OptState | None = None) -> OptState:
+    def _opt_state(self, problem, sv: DeviceSolver, prev: OptState | None = None) -> OptState:
         s = sv.read()
         f0 = prev.line_search_state.f_alpha if prev is not None else s.energy
         done = s.result != Result.UNKNOWN_ERROR
+        dof_map = problem.model.dof_map
+        direction = dof_map.to_free(sv.read_direction().to(dof_map.free_indices.device))
         return OptState(
             n_steps=s.n_steps,
             line_search_state=LineSearchState(s.alpha, f0, s.energy, s.line_search_steps, s.line_search_ok),
@@ -259,4 +289,6 @@ class PNCG:
             beta=s.beta,
             done=done,
             result=s.result,
+            direction=direction,
+            hess_damping_state=HessDampingState(0.0, s.hess_diag_mean),
         )

@@ -217,6 +217,9 @@ typedef struct agb_pncg_stats {
   double beta;                 /* last beta */
   int32_t line_search_steps;   /* halvings in the last line search */
   int32_t line_search_ok;
+  double hess_diag_mean;       /* mean of the positive free Hessian-diagonal entries at the
+                                  returned u: the preconditioner's fill for zero entries
+                                  (1 when there are none) */
 } agb_pncg_stats;
 
 void agb_pncg_default_params(agb_pncg_params* params);
@@ -242,6 +245,13 @@ int agb_solver_step(agb_solver* solver, void* stream);
 int agb_solver_step_kernels(agb_solver* solver, int32_t* n_kernels);
 /* copy u out (device, caller order) and the stats (host); synchronises stream */
 int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
+/* the search direction p of the last iteration (the step taken was
+ * alpha * p; zero after agb_solver_reset and on fixed components), copied to
+ * HOST memory in caller order, n_points x 3 of the solver precision
+ * (PNCG state `direction`, exp/2026/05/06/toy/src/
+ * 20-ext-force-stable-neo-hookean-collision.py:211-224).  Synchronises the
+ * stream; AGB_E_INVALID before the first agb_solver_reset / agb_solver_load. */
+int agb_solver_read_direction(agb_solver* solver, void* p_host, void* stream);
 
 /* Checkpoint / resume of a solve (the reference has none; its experiments
  * restart from saved .vtu states).  A checkpoint is the solver's whole PNCG

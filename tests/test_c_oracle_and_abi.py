@@ -2,8 +2,11 @@
 the C ABI library (loads, exports every declared symbol, host-only entry
 points)."""
 
+import ctypes
 import pathlib
 import re
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -92,6 +95,42 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(lib, name), name
     assert set(declared) == set(_lib.exported_symbols())
+
+
+_STRUCTS = {"agb_pncg_params": _lib.PncgParams, "agb_pncg_stats": _lib.PncgStats,
+            "agb_cg_params": _lib.CgParams, "agb_cg_stats": _lib.CgStats}
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every struct the Python layer passes through the C ABI has the
+    header's size and field offsets (a C program built against the header
+    prints them)."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "apple_gb300.h"', "int main(void) {"]
+    for name, cls in _STRUCTS.items():
+        lines.append(f'  printf("{name} size %zu\\n", sizeof({name}));')
+        for field, _ in cls._fields_:
+            lines.append(f'  printf("{name} {field} %zu\\n", offsetof({name}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line}
+    for name, cls in _STRUCTS.items():
+        assert got[(name, "size")] == ctypes.sizeof(cls), name
+        for field, _ in cls._fields_:
+            assert got[(name, field)] == getattr(cls, field).offset, (name, field)
+    # and the header declares no field the Python struct lacks
+    h = (ROOT / "include/apple_gb300.h").read_text()
+    for name, cls in _STRUCTS.items():
+        body = re.search(r"typedef struct " + name + r" \{(.*?)\} " + name + ";", h, re.S).group(1)
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        fields = re.findall(r"^\s*\w+\s+(\w+);", body, re.M)
+        assert fields == [f for f, _ in cls._fields_], name
 
 
 def test_region_compute_host_entry_point():
