@@ -686,13 +686,16 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   // one material per solver; stable Neo-Hookean and muscle potentials mix as
   // muscles (a stable Neo-Hookean cell is a muscle cell with zero activation)
   bool any_arap = false, any_snh = false, any_muscle = false;
+  int64_t n_cells = 0;
   for (agb_fem* f : m->fems) {
+    n_cells += f->plan.n_cells;
     any_arap |= f->material == AGB_ARAP;
     any_snh |= f->material == AGB_STABLE_NEO_HOOKEAN;
     any_muscle |= f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
   }
   AGB_REQUIRE(!(any_arap && (any_snh || any_muscle)), AGB_E_INVALID,
               "agb_solver_create: ARAP and stable Neo-Hookean potentials cannot share a solver");
+  AGB_REQUIRE(n_cells > 0, AGB_E_INVALID, "agb_solver_create: the model's FEM potentials have no cells");
   const int mat = any_arap ? AGB_ARAP : (any_muscle ? AGB_STABLE_NEO_HOOKEAN_MUSCLE : AGB_STABLE_NEO_HOOKEAN);
   agb_pncg_params prm;
   agb_pncg_default_params(&prm);

@@ -114,3 +114,16 @@ def test_free_dofs_without_stiffness(cuda_device):
     sol = fwd.step()
     assert sol.result == ag.Result.PRIMARY_SUCCESS, sol
     assert torch.equal(fwd.state.u, u0)
+
+
+def test_solver_rejects_a_model_without_cells(cuda_device):
+    """A model whose only FEM potential has no cells has nothing to iterate:
+    the solver is refused at creation with a status, not at the first launch."""
+    m = meshgen.grid(2, 2, 2)
+    empty = ag.with_lame(meshgen.TetMesh(m.points, np.zeros((0, 4), np.int32)), 1.0e3, 1.0e4)
+    b = ag.ModelBuilder()
+    b.add_vertices(meshgen.TetMesh(m.points, m.cells))
+    b.add_potential(ag.StableNeoHookean.from_pyvista(empty))
+    model = b.finalize()
+    with pytest.raises(RuntimeError, match="no cells"):
+        ag.PNCG().solver(ag.ForwardProblem(model))

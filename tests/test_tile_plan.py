@@ -67,3 +67,9 @@ def test_plan_rejects_bad_connectivity():
     bad[0, 0] = m.n_points
     with pytest.raises(RuntimeError):
         _plan(meshgen.TetMesh(m.points, bad))
+
+
+def test_plan_of_no_cells_is_empty():
+    m = meshgen.grid(2, 2, 2)
+    nt, ng, tile, group, slots = _plan(meshgen.TetMesh(m.points, np.zeros((0, 4), np.int32)))
+    assert nt == 0 and ng == 0 and tile.size == 0
