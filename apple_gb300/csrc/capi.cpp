@@ -1273,9 +1273,13 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
     agb_model* m = models[k];
     AGB_REQUIRE(m && !m->fems.empty(), AGB_E_INVALID, "agb_batch_create: model %d has no FEM potential", k);
     AGB_REQUIRE(m->precision == prec, AGB_E_INVALID, "agb_batch_create: models must share a precision");
-    for (agb_fem* f : m->fems)
+    int64_t n_cells = 0;
+    for (agb_fem* f : m->fems) {
       AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN || f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE,
                   AGB_E_INVALID, "agb_batch_create: the batched form runs stable Neo-Hookean and muscle potentials");
+      n_cells += f->plan.n_cells;
+    }
+    AGB_REQUIRE(n_cells > 0, AGB_E_INVALID, "agb_batch_create: model %d: its FEM potentials have no cells", k);
   }
   // with any muscle potential every cell runs as a muscle cell (zero activation
   // for the stable Neo-Hookean ones)

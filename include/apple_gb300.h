@@ -227,8 +227,9 @@ void agb_pncg_default_params(agb_pncg_params* params);
 /* A PNCG solver over the model (Forward.step / Optimizer.minimize,
  * forward/_forward.py:52-56).  The model's FEM potentials must be all ARAP, or
  * all stable Neo-Hookean and muscle (mixed ones run as muscle cells, the
- * stable Neo-Hookean ones with zero activation).  A single FEM potential's
- * element records are used in place; several are copied and concatenated. */
+ * stable Neo-Hookean ones with zero activation), with at least one cell
+ * among them (AGB_E_INVALID otherwise).  A single FEM potential's element
+ * records are used in place; several are copied and concatenated. */
 int agb_solver_create(agb_model* model, const agb_pncg_params* params, agb_solver** out);
 int agb_solver_destroy(agb_solver* solver);
 /* load u (device, full vector; fixed components are overwritten by the
@@ -278,7 +279,8 @@ int agb_pncg_minimize_host(agb_solver* solver, void* u_host, agb_pncg_stats* sta
 
 /* ---------------------------------------------------------------------------
  * Batched PNCG: independent models (each its own space, stable Neo-Hookean
- * potentials of one precision, fixed DOFs, external force) solved together.
+ * or muscle potentials of one precision with at least one cell, fixed DOFs,
+ * external force) solved together.
  * Every model runs the PNCG iteration above with its own beta, step and
  * termination; an iteration of all running models is one set of launches
  * (one CUDA graph).  No reference counterpart: the reference steps one
