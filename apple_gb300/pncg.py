@@ -17,6 +17,7 @@ from __future__ import annotations
 import ctypes
 import dataclasses
 import enum
+import weakref
 
 import torch
 
@@ -219,7 +220,6 @@ class PNCG:
         # reference gradient each time ||g|| drops by this factor; 0: off;
         # < 0: on (1e-2) when rtol < 1e-5 asks for more than FP32 forces resolve
         self.refresh_ratio = refresh_ratio
-        self._solvers: dict[int, DeviceSolver] = {}
 
     def params(self, dtype) -> _lib.PncgParams:
         p = _lib.PncgParams()
@@ -242,10 +242,13 @@ class PNCG:
         wm = getattr(model, "warp_model", None)
         if wm is None or not hasattr(wm, "handle"):
             raise TypeError("PNCG runs on apple_gb300 models (ForwardProblem over a Model)")
-        key = id(wm)
-        if key not in self._solvers:
-            self._solvers[key] = DeviceSolver(wm, self.params(wm.dtype))
-        return self._solvers[key]
+        # one device solver per (model, optimizer): cached on the model and
+        # keyed weakly by the optimizer, so it is freed with either of them
+        cache = wm.__dict__.setdefault("_pncg_solvers", weakref.WeakKeyDictionary())
+        sv = cache.get(self)
+        if sv is None:
+            sv = cache[self] = DeviceSolver(wm, self.params(wm.dtype))
+        return sv
 
     # -- Optimizer.minimize (forward/_forward.py:52-56) ------------------------
     def minimize(self, problem, state, free: torch.Tensor):
