@@ -11,6 +11,7 @@ shape (1,).  Every method runs the native sm_103a kernels of
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import numpy as np
 import torch
@@ -84,6 +85,19 @@ class Space:
             self.handle = None
 
 
+class _Owned:
+    """One C handle, destroyed with this wrapper (``destroy``: the C call)."""
+
+    def __init__(self, handle: ctypes.c_void_p, destroy: str):
+        self.handle = handle
+        self._destroy = destroy
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib._lib is not None:
+            getattr(_lib.load(), self._destroy)(self.handle)
+            self.handle = None
+
+
 class WarpPotential:
     """The energy-term interface of warp/model/_potential.py:9-32: every
     method accumulates into ``output`` (the caller zeroes it); the base
@@ -141,8 +155,9 @@ class WarpPotentialFem(WarpPotential):
         self.dtype = dtype
         self.tile_elems = int(tile_elems)
         self.requires_grad = tuple(requires_grad)
-        self._own = None  # (space, handle) for standalone use
-        self._by_space: dict[int, ctypes.c_void_p] = {}
+        self._own = None  # (space, owned handle) for standalone use
+        # one device copy per space, destroyed when its space goes
+        self._by_space: weakref.WeakKeyDictionary[Space, _Owned] = weakref.WeakKeyDictionary()
 
     # -- construction (warp/fem/_base.py:78-111) -------------------------------
     @classmethod
@@ -186,16 +201,21 @@ class WarpPotentialFem(WarpPotential):
 
     def on_space(self, space: Space) -> ctypes.c_void_p:
         """The device potential over ``space`` (created once per space)."""
-        key = id(space)
-        if key not in self._by_space:
-            self._by_space[key] = self._create(space)
-        return self._by_space[key]
+        owned = self._by_space.get(space)
+        if owned is None:
+            owned = self._by_space[space] = _Owned(self._create(space), "agb_fem_destroy")
+        return owned.handle
 
     def _standalone(self) -> ctypes.c_void_p:
         if self._own is None:
             space = Space(self.n_points, self.points)
-            self._own = (space, self._create(space))
-        return self._own[1]
+            self._own = (space, _Owned(self._create(space), "agb_fem_destroy"))
+        return self._own[1].handle
+
+    def _handles(self) -> list[ctypes.c_void_p]:
+        """Every device copy of this potential."""
+        out = [o.handle for o in list(self._by_space.values())]
+        return out + ([self._own[1].handle] if self._own is not None else [])
 
     def info(self) -> tuple[int, int]:
         nt, ntv = ctypes.c_int32(), ctypes.c_int32()
@@ -209,18 +229,6 @@ class WarpPotentialFem(WarpPotential):
         h = ctypes.c_uint32()
         _lib.call("agb_fem_cells", self._standalone(), out.ctypes.data, ctypes.byref(h))
         return out, h.value
-
-    def __del__(self):
-        if _lib._lib is None:
-            return
-        lib = _lib.load()
-        for h in getattr(self, "_by_space", {}).values():
-            lib.agb_fem_destroy(h)
-        own = getattr(self, "_own", None)
-        if own is not None:
-            lib.agb_fem_destroy(own[1])
-        self._by_space = {}
-        self._own = None
 
     # -- WarpPotential surface (warp/model/_potential.py:19-32) ----------------
     def fun(self, u: torch.Tensor, output: torch.Tensor) -> None:
@@ -344,7 +352,11 @@ class StableNeoHookeanMuscle(WarpPotentialFem):
 
     def _create(self, space: Space) -> ctypes.c_void_p:
         h = super()._create(space)
-        _lib.call("agb_fem_set_activation", h, self.activation.ctypes.data)
+        try:
+            _lib.call("agb_fem_set_activation", h, self.activation.ctypes.data)
+        except BaseException:
+            _lib.load().agb_fem_destroy(h)
+            raise
         return h
 
     def set_activation(self, activation) -> None:
@@ -353,8 +365,7 @@ class StableNeoHookeanMuscle(WarpPotentialFem):
         records at its next launch; a solver over several potentials copied
         the records when it was created and needs to be built again."""
         self.activation = _activation_array(activation, self.cells.shape[0])
-        handles = list(self._by_space.values()) + ([self._own[1]] if self._own is not None else [])
-        for h in handles:
+        for h in self._handles():
             _lib.call("agb_fem_set_activation", h, self.activation.ctypes.data)
 
     def grad_param_vjp(self, u: torch.Tensor, w: torch.Tensor) -> dict:
