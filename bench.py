@@ -304,9 +304,13 @@ def run_ours(a) -> None:
     peak, peak_kind = _measured_peak()
     achieved = per_launch[names[k]] / (ms[k] * 1e-3) / 1e9
     traffic = None
-    tp = ROOT / "profiles" / "traffic_per_launch.json"
-    if tp.exists():
-        traffic = json.loads(tp.read_text()).get(names[k])
+    # dram bytes per launch from one ncu capture of this workload (the
+    # small grid has none)
+    tp = ROOT / "profiles" / "traffic_passes_snh_grid_50x50x120_1.5M.json"
+    if tp.exists() and not a.small:
+        rec = json.loads(tp.read_text())
+        if rec.get("workload") == WORKLOAD:
+            traffic = rec.get(names[k])
 
     # the spec solve: PNCG from the initial state to ||g||/||g0|| <= 1e-6
     solve_opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=20000, rtol=1e-6))
