@@ -154,3 +154,13 @@ def test_c_abi_rejects_bad_mesh_without_gpu():
     with pytest.raises(_lib.AgbError, match="outside"):
         _lib.call("agb_region_compute", 1, cells.ctypes.data, 4, pts.ctypes.data, None, dh.ctypes.data,
                   dv.ctypes.data, ctypes.byref(ctypes.c_int32()))
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built library every entry raises."""
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", tmp_path / "libapple_gb300.so")
+    with pytest.raises(ImportError, match="no fallback"):
+        _lib.load()
+    with pytest.raises(ImportError):
+        _lib.call("agb_version")
