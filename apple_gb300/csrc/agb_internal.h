@@ -13,6 +13,8 @@
 namespace agb {
 
 void set_error(const char* fmt, ...);
+// forget the last message (calls that add a message only when none was set)
+void clear_error();
 
 #define AGB_CHECK_CUDA(call)                                                                  \
   do {                                                                                        \

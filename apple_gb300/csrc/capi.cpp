@@ -271,6 +271,7 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
                    const int32_t* cells, const double* points, const double* dhdX,
                    const double* dV, const double* fraction, const double* mu,
                    const double* lambda, int32_t tile_elems, agb_fem** out) {
+  clear_error();
   AGB_REQUIRE(out, AGB_E_INVALID, "agb_fem_create: out is null");
   *out = nullptr;
   AGB_REQUIRE(space, AGB_E_INVALID, "agb_fem_create: space is null");
@@ -367,6 +368,7 @@ int agb_fem_create(agb_space* space, int material, int precision, int32_t n_cell
   if (!rc) rc = dalloc(&f->d_counter, 1);
   if (!rc && cudaMemset(f->d_counter, 0, sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
   if (rc) {
+    if (rc == AGB_E_CUDA && agb::last_error()[0] == 0) set_error("agb_fem_create: CUDA allocation failed");
     agb_fem_destroy(f);
     return rc;
   }
@@ -516,6 +518,7 @@ int agb_model_destroy(agb_model* m) {
 int agb_model_create(agb_space* space, int precision, int32_t n_pot, agb_fem* const* pots,
                      const uint8_t* fixed_mask, const double* fixed_values, int32_t n_force,
                      const int32_t* force_index, const double* force, agb_model** out) {
+  clear_error();
   AGB_REQUIRE(out, AGB_E_INVALID, "agb_model_create: out is null");
   *out = nullptr;
   AGB_REQUIRE(space && n_pot >= 0 && (n_pot == 0 || pots), AGB_E_INVALID,
@@ -599,6 +602,7 @@ int agb_model_create(agb_space* space, int precision, int32_t n_pot, agb_fem* co
   if (!rc) rc = dalloc(&m->d_counter, 1);
   if (!rc && cudaMemset(m->d_counter, 0, sizeof(unsigned)) != cudaSuccess) rc = AGB_E_CUDA;
   if (rc) {
+    if (rc == AGB_E_CUDA && agb::last_error()[0] == 0) set_error("agb_model_create: CUDA allocation failed");
     agb_model_destroy(m);
     return rc;
   }
@@ -680,6 +684,7 @@ int agb_solver_destroy(agb_solver* sv) {
 }
 
 int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** out) {
+  clear_error();
   AGB_REQUIRE(out && m, AGB_E_INVALID, "agb_solver_create: null argument");
   *out = nullptr;
   AGB_REQUIRE(!m->fems.empty(), AGB_E_INVALID, "agb_solver_create: the model has no FEM potential");
@@ -1071,6 +1076,7 @@ int agb_solver_load(agb_solver* sv, const void* host, void* stream) {
 
 int agb_solver_time_passes(agb_solver* sv, int32_t reps, void* flush, size_t flush_bytes,
                            float* ms, void* stream) {
+  clear_error();
   AGB_REQUIRE(sv && ms && reps > 0, AGB_E_INVALID, "agb_solver_time_passes: bad argument");
   cudaStream_t s = as_stream(stream);
   cudaEvent_t e0, e1;
@@ -1123,6 +1129,7 @@ void agb_cg_default_params(agb_cg_params* p) {
 
 static int cg_setup(agb_solver* sv) {
   if (sv->d_cg) return AGB_OK;
+  clear_error();
   const int np = sv->args.n_points;
   const size_t v4 = v4_bytes(sv->precision);
   const int vblocks = sv->args.vblocks;
@@ -1266,6 +1273,7 @@ int agb_batch_destroy(agb_batch* b) {
 
 int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_params* params,
                      int32_t chunk_verts, agb_batch** out) {
+  clear_error();
   AGB_REQUIRE(out && n_models > 0 && models, AGB_E_INVALID, "agb_batch_create: bad arguments");
   *out = nullptr;
   const int prec = models[0]->precision;

@@ -32,6 +32,8 @@ void set_error(const char* fmt, ...) {
 
 const char* last_error() { return g_last_error.c_str(); }
 
+void clear_error() { g_last_error.clear(); }
+
 // 21 bits per axis interleaved into a 63-bit key.
 static inline uint64_t spread21(uint64_t v) {
   v &= 0x1fffffull;
