@@ -26,7 +26,7 @@ class _Recorder:
 
     def call(self, name, *args):
         self.calls.append((name, args))
-        if name in ("agb_space_create", "agb_fem_create"):
+        if name in ("agb_space_create", "agb_fem_create", "agb_model_create"):
             args[-1]._obj.value = self._new(name.split("_")[1])
         return 0
 
@@ -42,6 +42,8 @@ class _Recorder:
             return self._destroy("fem")
         if name == "agb_space_destroy":
             return self._destroy("space")
+        if name == "agb_model_destroy":
+            return self._destroy("model")
         raise AttributeError(name)
 
 
@@ -103,3 +105,30 @@ def test_set_activation_reaches_every_live_copy(rec):
     pot.set_activation(np.full((m.n_cells, 6), 0.01))
     got = {a[0].value for name, a in rec.calls if name == "agb_fem_set_activation"}
     assert got == hs
+
+
+def test_models_rebuilt_from_one_potential(rec):
+    """Two models built in turn from one potential: each is created over a
+    live device copy on its own space; the first copy goes with the first
+    model."""
+    from apple_gb300.model import WarpModel
+
+    pot, m = _pot()
+
+    def fems_of_last_model_create():
+        name, args = [c for c in rec.calls if c[0] == "agb_model_create"][-1]
+        n = args[2]
+        return [args[3][k] for k in range(n)]
+
+    wm1 = WarpModel({"e": pot}, m.n_points, m.points)
+    (f1,) = fems_of_last_model_create()
+    assert rec.live[f1] == "fem"
+    del wm1
+    gc.collect()
+    assert f1 not in rec.live and not any(k == "model" for k in rec.live.values())
+    wm2 = WarpModel({"e": pot}, m.n_points, m.points)
+    (f2,) = fems_of_last_model_create()
+    assert rec.live[f2] == "fem" and f2 != f1
+    del wm2
+    gc.collect()
+    assert not rec.live
