@@ -13,7 +13,8 @@ solved displacement) for pyvista/ParaView.
 Encodings follow the VTK XML file format: ``ascii``; ``binary`` (base64,
 inline) and ``appended`` (``raw`` or ``base64``) data, each with a UInt32 or
 UInt64 byte-count header, optionally zlib-compressed in blocks
-(``vtkZLibDataCompressor``).  Only tetrahedra (cell type 10) are read as
+(``vtkZLibDataCompressor``); little- or big-endian files (written
+little-endian).  Only tetrahedra (cell type 10) are read as
 cells; other cell types are skipped with their cell data.
 """
 
@@ -39,9 +40,12 @@ _NAMES = {np.dtype(v).str[1:]: k for k, v in _TYPES.items()}
 
 class _Ctx:
     def __init__(self, root: ET.Element, appended: bytes | None, appended_encoding: str):
-        if root.get("byte_order", "LittleEndian") != "LittleEndian":
-            raise ValueError("only little-endian .vtu files are supported")
-        self.hdr = np.uint64 if root.get("header_type", "UInt32") == "UInt64" else np.uint32
+        order = root.get("byte_order", "LittleEndian")
+        if order not in ("LittleEndian", "BigEndian"):
+            raise ValueError(f"unknown byte_order {order}")
+        self.order = "<" if order == "LittleEndian" else ">"
+        hdr = np.uint64 if root.get("header_type", "UInt32") == "UInt64" else np.uint32
+        self.hdr = np.dtype(hdr).newbyteorder(self.order)
         self.hsize = np.dtype(self.hdr).itemsize
         comp = root.get("compressor")
         if comp not in (None, "", "vtkZLibDataCompressor"):
@@ -109,7 +113,7 @@ class _Ctx:
 
 
 def _array(ctx: _Ctx, el: ET.Element) -> np.ndarray:
-    dt = np.dtype(_TYPES[el.get("type")]).newbyteorder("<")
+    dt = np.dtype(_TYPES[el.get("type")]).newbyteorder(ctx.order)
     nc = int(el.get("NumberOfComponents", "1"))
     fmt = el.get("format", "ascii")
     if fmt == "ascii":
@@ -120,7 +124,8 @@ def _array(ctx: _Ctx, el: ET.Element) -> np.ndarray:
         a = np.frombuffer(ctx.decode_appended(int(el.get("offset"))), dtype=dt)
     else:
         raise ValueError(f"unknown DataArray format {fmt}")
-    return a.reshape(-1, nc) if nc > 1 else a.copy()
+    a = a.astype(a.dtype.newbyteorder("="))  # native order, a copy
+    return a.reshape(-1, nc) if nc > 1 else a
 
 
 def read(path) -> TetMesh:

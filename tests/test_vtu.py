@@ -4,6 +4,7 @@ tetrahedra are kept, and a file feeds the region precompute and the
 potentials' from_pyvista."""
 
 import base64
+import zlib
 
 import numpy as np
 import pytest
@@ -38,18 +39,28 @@ def test_round_trip(tmp_path, fmt, compress):
         np.testing.assert_array_equal(r.cell_data[k].reshape(np.shape(v)), v)
 
 
-def _uint32_file(arrays, joint: bool) -> str:
-    """A hand-assembled inline-binary file with UInt32 headers."""
+def _uint32_file(arrays, joint: bool, big_endian: bool = False, compress: bool = False) -> str:
+    """A hand-assembled inline-binary file with UInt32 headers (in the
+    file's byte order, as is its data; compressed: one zlib block per array,
+    its header encoded on its own as VTK writes it)."""
+    o = ">" if big_endian else "<"
+
     def enc(a):
-        data = a.tobytes()
-        head = np.array([len(data)], np.uint32).tobytes()
+        data = a.astype(a.dtype.newbyteorder(o)).tobytes()
+        if compress:
+            z = zlib.compress(data)
+            head = np.array([1, len(data), len(data), len(z)], o + "u4").tobytes()
+            return base64.b64encode(head).decode() + base64.b64encode(z).decode()
+        head = np.array([len(data)], o + "u4").tobytes()
         if joint:
             return base64.b64encode(head + data).decode()
         return base64.b64encode(head).decode() + base64.b64encode(data).decode()
 
     pts, conn, offs, types, mu = arrays
+    order = "BigEndian" if big_endian else "LittleEndian"
+    comp = ' compressor="vtkZLibDataCompressor"' if compress else ""
     return f"""<?xml version="1.0"?>
-<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian" header_type="UInt32">
+<VTKFile type="UnstructuredGrid" version="0.1" byte_order="{order}" header_type="UInt32"{comp}>
  <UnstructuredGrid><Piece NumberOfPoints="{len(pts)}" NumberOfCells="{len(types)}">
   <CellData><DataArray type="Float64" Name="mu" format="binary">{enc(mu)}</DataArray></CellData>
   <Points><DataArray type="Float32" NumberOfComponents="3" format="binary">{enc(pts)}</DataArray></Points>
@@ -74,6 +85,20 @@ def test_uint32_headers_and_one_byte_arrays(tmp_path, joint):
     np.testing.assert_array_equal(r.cells, [[0, 1, 2, 3]])
     np.testing.assert_array_equal(r.points, pts.astype(np.float64))
     np.testing.assert_array_equal(r.cell_data["mu"], [2.5])
+
+
+@pytest.mark.parametrize("joint,compress", [(True, False), (False, False), (False, True)])
+def test_big_endian_files(tmp_path, joint, compress):
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1]], np.float32) * 0.75
+    conn = np.array([0, 1, 2, 3, 1, 2, 3, 4], np.int32)
+    arrays = (pts, conn, np.array([4, 8], np.int32), np.array([10, 10], np.uint8), np.array([2.5, -1.25]))
+    f = tmp_path / "be.vtu"
+    f.write_text(_uint32_file(arrays, joint, big_endian=True, compress=compress))
+    r = vtu.read(f)
+    np.testing.assert_array_equal(r.cells, [[0, 1, 2, 3], [1, 2, 3, 4]])
+    np.testing.assert_array_equal(r.points, pts.astype(np.float64))
+    np.testing.assert_array_equal(r.cell_data["mu"], [2.5, -1.25])
+    assert r.cell_data["mu"].dtype.isnative and r.points.dtype.isnative
 
 
 def test_only_tetrahedra_are_kept(tmp_path):
