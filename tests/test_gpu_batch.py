@@ -54,6 +54,8 @@ def test_batch_matches_plain_and_oracle(cuda_device, dtype):
         fwd = ag.Forward(_model(m, f, dtype), ag.PNCG(crit))
         psol = fwd.step()
         assert psol.result == ag.Result.PRIMARY_SUCCESS
+        # the preconditioner's diagonal mean at (nearly) the same equilibrium
+        assert sol.hess_diag_mean > 0 and abs(sol.hess_diag_mean / psol.hess_diag_mean - 1) < 1e-3
         err_plain = float((u.double() - fwd.state.u.double()).abs().max())
         # the FP64 oracle
         ora = O.FemPotential.from_mesh(O.Material.STABLE_NEO_HOOKEAN, m.points, m.cells,
