@@ -49,6 +49,7 @@ class _Recorder:
 
 @pytest.fixture
 def rec(monkeypatch):
+    gc.collect()  # earlier tests' handles go to the real library first
     r = _Recorder()
     monkeypatch.setattr(_lib, "call", r.call)
     monkeypatch.setattr(_lib, "load", lambda: r)

@@ -27,6 +27,7 @@ class _Problem:
 
 
 def _fake_solvers(monkeypatch):
+    gc.collect()  # earlier tests' solvers go before the stand-in takes over
     made = []
 
     class FakeSolver:
