@@ -120,7 +120,7 @@ _SIGNATURES = {
     "agb_solver_step_kernels": (c_int, [c_void_p, POINTER(c_int32)]),
     "agb_solver_checkpoint_size": (c_int, [c_void_p, POINTER(ctypes.c_size_t)]),
     "agb_solver_save": (c_int, [c_void_p, c_void_p, c_void_p]),
-    "agb_solver_load": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "agb_solver_load": (c_int, [c_void_p, c_void_p, ctypes.c_size_t, c_void_p]),
     "agb_fem_grad_activation_vjp": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 

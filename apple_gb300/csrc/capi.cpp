@@ -164,6 +164,62 @@ int ensure_vjp_tables(agb_fem* f) {
   return upload(f->d_vol, v.data(), 4 * v.size());
 }
 
+// 64-bit FNV-1a over byte ranges: the checkpoint fingerprint of a solver
+struct Fnv64 {
+  uint64_t h = 0xcbf29ce484222325ull;
+  void bytes(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+      h ^= c[i];
+      h *= 0x100000001b3ull;
+    }
+  }
+  template <class T>
+  void vec(const std::vector<T>& v) {
+    const uint64_t n = v.size();
+    bytes(&n, sizeof(n));
+    bytes(v.data(), v.size() * sizeof(T));
+  }
+  template <class T>
+  void val(const T& v) {
+    bytes(&v, sizeof(T));
+  }
+};
+
+// What a checkpoint depends on besides its sizes: the mesh of every potential
+// (tiles, corner ids, element geometry, mu dV, lambda dV), the fixed mask and
+// values, the external force per vertex and the solver parameters.  Muscle
+// activations are left out: they are a control input that
+// agb_fem_set_activation changes in place between solves.
+uint64_t solver_fingerprint(const agb_model* m, const agb_pncg_params& prm, int precision, int material) {
+  Fnv64 f;
+  f.val(precision);
+  f.val(material);
+  f.val(m->space->n_points);
+  f.vec(m->mask_internal);
+  f.vec(m->fixed_internal);
+  f.vec(m->force_internal);
+  for (const agb_fem* fe : m->fems) {
+    f.val(fe->material);
+    f.vec(fe->plan.tile_estart);
+    f.vec(fe->plan.tile_vstart);
+    f.vec(fe->plan.tv_vid);
+    f.vec(fe->plan.ids);
+    f.vec(fe->plan.D);
+    f.vec(fe->plan.mudv);
+    f.vec(fe->plan.lamdv);
+  }
+  f.val(prm.max_steps);
+  f.val(prm.rtol);
+  f.val(prm.atol);
+  f.val(prm.armijo_c);
+  f.val(prm.overstep);
+  f.val(prm.beta_max);
+  f.val(prm.max_backtracking);
+  f.val(prm.refresh_ratio);
+  return f.h;
+}
+
 }  // namespace
 
 FemView agb_fem::view() const {
@@ -714,6 +770,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   sv->model = m;
   sv->params = prm;
   sv->precision = m->precision;
+  sv->fingerprint = solver_fingerprint(m, prm, m->precision, mat);
   const int np = m->space->n_points;
   int rc = AGB_OK;
   // element data: one potential is used in place; several are concatenated
@@ -1013,8 +1070,10 @@ int agb_solver_read_direction(agb_solver* sv, void* p_host, void* stream) {
 struct CheckpointHeader {
   uint64_t magic;
   int32_t version, precision, n_points, delta, state_bytes, pad;
+  uint64_t fingerprint;  // solver_fingerprint of the saving solver
 };
 constexpr uint64_t kCheckpointMagic = 0x4147424350544b31ull;  // "AGBCPTK1"
+constexpr int32_t kCheckpointVersion = 2;
 
 static size_t checkpoint_vec_bytes(const agb_solver* sv) {
   const size_t v4 = v4_bytes(sv->precision) * (size_t)sv->args.n_points;
@@ -1041,8 +1100,8 @@ static std::vector<std::pair<void*, size_t>> checkpoint_arrays(agb_solver* sv) {
 int agb_solver_save(agb_solver* sv, void* host, void* stream) {
   AGB_REQUIRE(sv && host, AGB_E_INVALID, "agb_solver_save: null argument");
   cudaStream_t s = as_stream(stream);
-  CheckpointHeader h{kCheckpointMagic, 1, sv->precision, sv->args.n_points, sv->args.delta,
-                     (int32_t)sizeof(SolverState), 0};
+  CheckpointHeader h{kCheckpointMagic, kCheckpointVersion, sv->precision, sv->args.n_points, sv->args.delta,
+                     (int32_t)sizeof(SolverState), 0, sv->fingerprint};
   std::memcpy(host, &h, sizeof(h));
   char* dst = static_cast<char*>(host) + sizeof(h);
   for (const auto& [ptr, n] : checkpoint_arrays(sv)) {
@@ -1053,16 +1112,27 @@ int agb_solver_save(agb_solver* sv, void* host, void* stream) {
   return AGB_OK;
 }
 
-int agb_solver_load(agb_solver* sv, const void* host, void* stream) {
+int agb_solver_load(agb_solver* sv, const void* host, size_t bytes, void* stream) {
+  clear_error();
   AGB_REQUIRE(sv && host, AGB_E_INVALID, "agb_solver_load: null argument");
+  const size_t expect = sizeof(CheckpointHeader) + checkpoint_vec_bytes(sv) + sizeof(SolverState);
+  AGB_REQUIRE(bytes >= sizeof(CheckpointHeader), AGB_E_INVALID,
+              "agb_solver_load: %zu bytes is shorter than a checkpoint header", bytes);
   CheckpointHeader h;
   std::memcpy(&h, host, sizeof(h));
-  AGB_REQUIRE(h.magic == kCheckpointMagic && h.version == 1, AGB_E_INVALID, "agb_solver_load: not a checkpoint");
+  AGB_REQUIRE(h.magic == kCheckpointMagic && h.version == kCheckpointVersion, AGB_E_INVALID,
+              "agb_solver_load: not a checkpoint of this version");
+  AGB_REQUIRE(bytes == expect, AGB_E_INVALID,
+              "agb_solver_load: buffer of %zu bytes, this solver's checkpoints have %zu", bytes, expect);
   AGB_REQUIRE(h.precision == sv->precision && h.n_points == sv->args.n_points && h.delta == sv->args.delta &&
                   h.state_bytes == (int32_t)sizeof(SolverState),
               AGB_E_INVALID,
               "agb_solver_load: checkpoint of another solver (precision %d, %d points, correction %d)",
               h.precision, h.n_points, h.delta);
+  AGB_REQUIRE(h.fingerprint == sv->fingerprint, AGB_E_INVALID,
+              "agb_solver_load: checkpoint of another model or parameter set (fingerprint %016llx, "
+              "this solver %016llx)",
+              (unsigned long long)h.fingerprint, (unsigned long long)sv->fingerprint);
   cudaStream_t s = as_stream(stream);
   const char* src = static_cast<const char*>(host) + sizeof(h);
   for (const auto& [ptr, n] : checkpoint_arrays(sv)) {

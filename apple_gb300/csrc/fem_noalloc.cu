@@ -19,8 +19,6 @@
 // it keeps the last call's contents: the counter is cleared before each
 // launch and every partial is written before it is read.  Calls that overlap
 // on the GPU (concurrent streams) race on the array.
-#include <mutex>
-
 #include "kernels.h"
 #include "tile.cuh"
 
@@ -75,23 +73,16 @@ __global__ void __launch_bounds__(kElemThreads)
     *out += tot[0];
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current (the array's name is only a host-side stand-in).
+// Device address of the scratch array.  The array's name is only a host-side
+// stand-in, so the address is looked up with the caller's device current, on
+// every call: the lookup is cheap once the module is loaded, and a cached
+// address would dangle after cudaDeviceReset reloads the module.
 static int noalloc_scratch(unsigned char** ptr) {
-  static std::mutex mu;
-  static void* addr[64] = {};
-  int dev = 0;
-  AGB_CHECK_CUDA(cudaGetDevice(&dev));
-  AGB_REQUIRE(dev >= 0 && dev < 64, AGB_E_INVALID, "agb_fem_fun_noalloc: device %d out of range", dev);
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_fun_noalloc_scratch);
-    AGB_REQUIRE(e == cudaSuccess && p, AGB_E_CUDA, "agb_fem_fun_noalloc: cudaGetSymbolAddress: %s",
-                cudaGetErrorString(e));
-    addr[dev] = p;
-  }
-  *ptr = (unsigned char*)addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_fun_noalloc_scratch);
+  AGB_REQUIRE(e == cudaSuccess && p, AGB_E_CUDA, "agb_fem_fun_noalloc: cudaGetSymbolAddress: %s",
+              cudaGetErrorString(e));
+  *ptr = (unsigned char*)p;
   return AGB_OK;
 }
 
@@ -100,6 +91,7 @@ static int noalloc_scratch(unsigned char** ptr) {
 using namespace agb;
 
 extern "C" int agb_fem_fun_noalloc(agb_fem* fem, const void* u, double* output, void* stream) {
+  clear_error();
   AGB_REQUIRE(fem && u && output, AGB_E_INVALID, "agb_fem_fun_noalloc: null argument");
   const FemView fv = fem->view();
   AGB_REQUIRE(fv.material != AGB_STABLE_NEO_HOOKEAN_MUSCLE, AGB_E_INVALID,

@@ -245,6 +245,7 @@ struct agb_solver {
   int step_kernels = 0;  // kernel nodes of one iteration
   cudaStream_t capture_stream = nullptr;
   bool has_state = false;  // vertex state written (reset or checkpoint load)
+  uint64_t fingerprint = 0;  // of the model and parameters, checked by agb_solver_load
 };
 
 struct agb_batch {

@@ -166,9 +166,16 @@ class DeviceSolver:
         return blob
 
     def load_state(self, blob: torch.Tensor) -> None:
-        """Restore a checkpoint; the next iterate() continues from it."""
+        """Restore a checkpoint; the next iterate() continues from it.  A
+        blob of the wrong length, or saved by a solver over another model or
+        with other parameters, raises RuntimeError and changes nothing."""
         blob = blob.to(dtype=torch.uint8, device="cpu").contiguous()
-        _lib.call("agb_solver_load", self.handle, ctypes.c_void_p(blob.data_ptr()), stream_ptr())
+        n = ctypes.c_size_t()
+        _lib.call("agb_solver_checkpoint_size", self.handle, ctypes.byref(n))
+        if blob.numel() != n.value:
+            raise RuntimeError(f"checkpoint of {blob.numel()} bytes; this solver's checkpoints have {n.value}")
+        _lib.call("agb_solver_load", self.handle, ctypes.c_void_p(blob.data_ptr()), ctypes.c_size_t(blob.numel()),
+                  stream_ptr())
 
     def read_direction(self) -> torch.Tensor:
         """The last iteration's search direction p (full (n_points, 3), CPU

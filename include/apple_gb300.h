@@ -154,9 +154,11 @@ int agb_fem_hess_quad(agb_fem* fem, const void* u, const void* p, double* output
  * the device up front) or a loop with a fixed memory budget: u is read in
  * the caller's order and the per-block partial sums and completion counter
  * live in one file-scope device array of 512 KiB + 256 B, which holds meshes
- * of at most 65,536 tiles (larger meshes: AGB_E_INVALID).  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  All calls on a device
+ * of at most 65,536 tiles (larger meshes: AGB_E_INVALID).  Every call looks
+ * up the array's device address (cudaGetSymbolAddress) with the caller's
+ * device current, so the address stays valid across cudaDeviceReset; the
+ * first call on a device may load the module, so make that first call
+ * before any stream capture.  Muscle potentials: AGB_E_INVALID.  All calls on a device
  * share the array; calls that overlap on the GPU race on it.  Accumulates
  * into output[0] like agb_fem_fun. */
 int agb_fem_fun_noalloc(agb_fem* fem, const void* u, double* output, void* stream);
@@ -259,13 +261,18 @@ int agb_solver_read_direction(agb_solver* solver, void* p_host, void* stream);
  * state -- positions as float-float pairs, gradient, Hessian diagonal, both
  * search directions, the reference state of the FP32 correction and the
  * scalar state -- in a host buffer of agb_solver_checkpoint_size bytes.
- * agb_solver_load accepts a checkpoint of a solver with the same vertex
- * count, precision and correction setting (AGB_E_INVALID otherwise); the
- * next agb_solver_iterate continues the solve exactly where it was saved.
- * Both synchronise the stream. */
+ * The header carries a fingerprint of the model and parameters (each
+ * potential's tiles, corner ids, element geometry and Lame parameters, the
+ * fixed mask and values, the external force, every agb_pncg_params field;
+ * muscle activations are not part of it).  agb_solver_load takes the
+ * buffer's length and accepts only a checkpoint of exactly that size whose
+ * precision, vertex count, correction setting and fingerprint match this
+ * solver's (AGB_E_INVALID otherwise, before anything is copied); the next
+ * agb_solver_iterate continues the solve exactly where it was saved.  Both
+ * synchronise the stream. */
 int agb_solver_checkpoint_size(agb_solver* solver, size_t* bytes);
 int agb_solver_save(agb_solver* solver, void* host, void* stream);
-int agb_solver_load(agb_solver* solver, const void* host, void* stream);
+int agb_solver_load(agb_solver* solver, const void* host, size_t bytes, void* stream);
 /* Diagnostics: time each pass of an iteration on its own with CUDA events on
  * `stream`, `reps` launches each (direction, gradient, vertex pass), writing
  * `flush_bytes` of the device buffer `flush` (may be NULL) before every launch

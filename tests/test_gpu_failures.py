@@ -16,19 +16,19 @@ from apple_gb300.forward import ModelState
 pytestmark = pytest.mark.gpu
 
 
-def _column(n=(4, 4, 6), dtype=torch.float32, extra_points=0, fix_all_mesh=False):
+def _column(n=(4, 4, 6), dtype=torch.float32, extra_points=0, fix_all_mesh=False, fixed_face=("z", "min"), E=1e4):
     m = meshgen.grid(*n)
     pts = m.points
     if extra_points:
         pts = np.concatenate([pts, 5.0 + np.arange(3 * extra_points, dtype=float).reshape(-1, 3)])
     n_pts = pts.shape[0]
-    lam, mu = meshgen.lame_converter(1e4, 0.45)
+    lam, mu = meshgen.lame_converter(E, 0.45)
     mesh = ag.with_lame(meshgen.TetMesh(pts, m.cells), mu, lam)
     mask = np.zeros((n_pts, 3), bool)
     if fix_all_mesh:
         mask[: m.n_points] = True
     else:
-        mask[: m.n_points][meshgen.face_mask(m, 2, "min")] = True
+        mask[: m.n_points][meshgen.face_mask(m, "xyz".index(fixed_face[0]), fixed_face[1])] = True
     mesh.point_data["FixedMask"] = mask
     mesh.point_data["FixedValue"] = np.zeros((n_pts, 3))
     b = ag.ModelBuilder(dtype=dtype)
@@ -85,6 +85,34 @@ def test_checkpoint_rejected_by_another_solver(cuda_device):
     bad[:8] = 0  # not a checkpoint
     with pytest.raises(RuntimeError):
         sa.load_state(bad)
+    good = sa.save_state()
+    with pytest.raises(RuntimeError, match="bytes"):
+        sa.load_state(good[:-1])  # truncated
+    with pytest.raises(RuntimeError, match="bytes"):
+        sa.load_state(torch.cat([good, torch.zeros(8, dtype=torch.uint8)]))  # trailing data
+    sa.load_state(good)  # the intact blob still loads
+
+
+def test_checkpoint_rejected_by_a_model_of_the_same_size(cuda_device):
+    """Same vertex count, precision and correction setting, but another fixed
+    face, another material or other solver parameters: the fingerprint in the
+    header refuses the checkpoint."""
+    base = _column(n=(4, 4, 6))
+    opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=1000, rtol=1e-7))
+    sa = opt.solver(ag.ForwardProblem(base))
+    sa.reset(ag.Forward(base, opt).state.u)
+    sa.iterate(5)
+    blob = sa.save_state()
+    other_face = _column(n=(4, 4, 6), fixed_face=("z", "max"))
+    stiffer = _column(n=(4, 4, 6), E=2e4)
+    for model, crit in ((other_face, dict(rtol=1e-7)), (stiffer, dict(rtol=1e-7)), (base, dict(rtol=1e-8))):
+        o = ag.PNCG(ag.ConvergenceCriteria(max_steps=1000, **crit))
+        sv = o.solver(ag.ForwardProblem(model))
+        with pytest.raises(RuntimeError, match="another model"):
+            sv.load_state(blob)
+    # an identically built model and solver accept it
+    o = ag.PNCG(ag.ConvergenceCriteria(max_steps=1000, rtol=1e-7))
+    o.solver(ag.ForwardProblem(_column(n=(4, 4, 6)))).load_state(blob)
 
 
 def test_nan_input_ends_with_nan_encountered(cuda_device):

@@ -51,3 +51,54 @@ def test_fun_noalloc_matches_fun_twice(cls, dtype, cuda_device):
         torch.cuda.synchronize(cuda_device)
         got = out.item() - 3.0
         assert got == pytest.approx(ref.item(), rel=TOL[dtype]), f"call {call}"
+
+
+def _call_noalloc(handle, U, out, stream):
+    _lib.call("agb_fem_fun_noalloc", handle, ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(out.data_ptr()), stream)
+
+
+def test_fun_noalloc_rejects_a_muscle(cuda_device):
+    """The muscle's activation stream is not read by this entry point, so it
+    refuses muscle potentials with a status instead of a wrong energy."""
+    m = meshgen.grid(3, 3, 3)
+    lam, mu = meshgen.lame_converter(1e4, 0.45)
+    mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells), mu, lam)
+    mesh.cell_data["activation"] = np.zeros((m.n_cells, 6))
+    pot = ag.StableNeoHookeanMuscle.from_pyvista(mesh)
+    U = torch.zeros((m.n_points, 3), dtype=torch.float32, device=cuda_device)
+    out = torch.zeros(1, dtype=torch.float64, device=cuda_device)
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    with pytest.raises(RuntimeError, match="muscle"):
+        _call_noalloc(pot._standalone(), U, out, stream)
+    torch.cuda.synchronize(cuda_device)
+    assert out.item() == 0.0
+
+
+def test_fun_noalloc_tile_limit(cuda_device):
+    """One element per tile: 65,536 cells fill the scratch array exactly and
+    match agb_fem_fun; one cell more is refused before any launch."""
+    m = meshgen.grid(30, 30, 16)  # 72,000 cells
+    lam, mu = meshgen.lame_converter(1e4, 0.45)
+    rng = np.random.default_rng(11)
+    u = 0.01 * rng.normal(size=(m.n_points, 3))
+    U = torch.tensor(u, dtype=torch.float32, device=cuda_device)
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    for n_cells, fits in ((65536, True), (65537, False)):
+        mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells[:n_cells]), mu, lam)
+        pot = ag.StableNeoHookean.from_pyvista(mesh, tile_elems=1)
+        handle = pot._standalone()
+        n_tiles = ctypes.c_int32()
+        _lib.call("agb_fem_info", handle, ctypes.byref(n_tiles), None)
+        assert n_tiles.value == n_cells
+        out = torch.zeros(1, dtype=torch.float64, device=cuda_device)
+        if fits:
+            ref = torch.zeros(1, dtype=torch.float64, device=cuda_device)
+            _lib.call("agb_fem_fun", handle, ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(ref.data_ptr()), stream)
+            _call_noalloc(handle, U, out, stream)
+            torch.cuda.synchronize(cuda_device)
+            assert out.item() == pytest.approx(ref.item(), rel=TOL[torch.float32])
+        else:
+            with pytest.raises(RuntimeError, match="65536"):
+                _call_noalloc(handle, U, out, stream)
+            torch.cuda.synchronize(cuda_device)
+            assert out.item() == 0.0
