@@ -24,15 +24,20 @@ kernels in double precision (the reference's default, ``JAX_ENABLE_X64``):
 * PNCG iteration (Dai-Kou beta, Jacobi preconditioner, alpha from pHp,
   Armijo backtracking)                    -- ``benches/bench_pncg_branching_backends.py:254-456,606-679``
 
-Parity pinning: the reference cannot run in this environment (Warp, JAX and
-the PNCG package ``liblaf-peach`` are absent), so this oracle is pinned by the
-reference's own known answers -- the embedded-vertex ARAP solve of
+Parity pinning: the reference's element path is pinned by golden vectors of
+its own code.  ``tests/golden/make_elem_golden.py`` runs the reference's
+unmodified ``warp/fem/_base.py`` kernels, the three materials, the element
+functions of ``warp/fem/func`` / ``warp/math`` and ``Region.compute_grad`` on
+NumPy (a stand-in for ``warp``, ``tests/golden/warp_numpy.py``), and
+``tests/test_golden_reference.py`` checks this oracle against them at 1e-12
+(energy density, PK1, fun, grad, hess_diag, hess_prod -- ARAP's as written
+and as intended -- hess_quad, dhdX, dV).  The end-to-end PNCG solve is pinned
+by the reference's known answer, the embedded-vertex ARAP solve of
 ``tests/forward/test_static_simulation.py:58-93`` (u4 = (0.05,-0.025,0.0375),
-atol 1e-8) and the lumped-volume sum of ``benches/test_aggregation.py:82,129``
--- plus finite-difference consistency of every derivative.  The stable
-Neo-Hookean element values and the PNCG iterate sequence have no golden vector
-in the reference: for those, parity is partial (finite differences and
-analytic identities only).
+atol 1e-8), and the scatter by the lumped-volume sum of
+``benches/test_aggregation.py:82,129``.  The PNCG iterate sequence of the
+real solver (``liblaf-peach``, not vendored) has no golden vector: it follows
+the in-tree proxy and stays unpinned.
 
 The 3x3 SVD uses LAPACK (``numpy.linalg.svd``) with the rotation-variant sign
 fix (det U = det V = +1, the smallest singular value carries the sign of

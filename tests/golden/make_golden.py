@@ -6,7 +6,9 @@ geometry, boundary conditions and expected answer of
 ``tests/forward/test_static_simulation.py`` (mesh 16-55, boundary values
 69-76, assertions 85-93).  Run it only where the reference tree is present:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path-to-liblaf-apple>
+
+or with ``APPLE_REFERENCE_ROOT`` set.
 
 Nothing at test time reads the reference tree; tests read the JSON.
 """
@@ -15,6 +17,7 @@ from __future__ import annotations
 
 import ast
 import json
+import os
 import pathlib
 import re
 import sys
@@ -61,4 +64,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("APPLE_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("usage: make_golden.py <path-to-liblaf-apple> (or set APPLE_REFERENCE_ROOT)")
+    main(root)
