@@ -104,6 +104,8 @@ _SIGNATURES = {
     "agb_solver_step": (c_int, [c_void_p, c_void_p]),
     "agb_solver_read": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_solver_read_direction": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "agb_solver_read_gradient": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "agb_solver_read_reductions": (c_int, [c_void_p, POINTER(c_double), c_void_p]),
     "agb_pncg_minimize_host": (c_int, [c_void_p, c_void_p, POINTER(PncgStats), c_void_p]),
     "agb_solver_time_passes": (c_int, [c_void_p, c_int32, c_void_p, ctypes.c_size_t, POINTER(ctypes.c_float), c_void_p]),
     "agb_batch_create": (c_int, [c_int32, c_void_p, POINTER(PncgParams), c_int32, POINTER(c_void_p)]),

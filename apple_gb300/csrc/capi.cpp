@@ -915,6 +915,9 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.vblocks = vblocks;
   a.max_bt = prm.max_backtracking;
   a.cond = 0;
+  a.cond_refresh = 0;
+  a.cond_outer = 0;
+  a.refresh_exits = 0;
   *out = sv;
   return AGB_OK;
 }
@@ -934,55 +937,119 @@ int agb_solver_reset(agb_solver* sv, const void* u, void* stream) {
   return AGB_OK;
 }
 
-// Capture one solver iteration into `graph` (which is being built: the
-// while body, or a top-level graph).  With the reference-state correction the
-// two refresh passes follow the vertex pass; they return at once unless the
-// vertex pass asked for a refresh.
-static cudaError_t capture_iteration(agb_solver* sv, cudaGraph_t graph, unsigned long long cond) {
+// Capture into `graph` after `deps` (which may be empty): the three passes
+// of one iteration (refresh = false) or the two refresh passes as plain
+// launches (refresh = true).
+static cudaError_t capture_into(agb_solver* sv, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t n_deps,
+                                const SolveArgs& a, bool refresh) {
   cudaStream_t cs = sv->capture_stream;
-  SolveArgs a = sv->args;
-  a.cond = cond;
-  cudaError_t e = cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  cudaError_t e = cudaStreamBeginCaptureToGraph(cs, graph, deps, nullptr, n_deps, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  cudaError_t le = launch_solver_iteration(a, cond != 0, cs);
-  if (le == cudaSuccess && a.delta) le = launch_solver_refresh(a, cs);
+  cudaError_t le = refresh ? launch_solver_refresh(a, cs, false) : launch_solver_iteration(a, a.cond != 0, cs);
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(cs, &captured);
   return e == cudaSuccess ? le : e;
 }
 
-static int build_loop_graph(agb_solver* sv) {
-  cudaGraph_t g = nullptr;
-  AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
-  cudaGraphConditionalHandle h;
-  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
-  if (e != cudaSuccess) {
-    cudaGraphDestroy(g);
-    return check_launch(e, "cudaGraphConditionalHandleCreate");
+// the nodes of `graph` that no other node depends on
+static cudaError_t graph_leaves(cudaGraph_t g, std::vector<cudaGraphNode_t>* leaves) {
+  size_t n = 0;
+  cudaError_t e = cudaGraphGetNodes(g, nullptr, &n);
+  if (e != cudaSuccess) return e;
+  std::vector<cudaGraphNode_t> nodes(n);
+  e = cudaGraphGetNodes(g, nodes.data(), &n);
+  for (size_t i = 0; e == cudaSuccess && i < n; ++i) {
+    size_t nd = 0;
+    e = cudaGraphNodeGetDependentNodes(nodes[i], nullptr, nullptr, &nd);
+    if (e == cudaSuccess && nd == 0) leaves->push_back(nodes[i]);
   }
+  return e;
+}
+
+static cudaError_t add_conditional(cudaGraph_t g, const cudaGraphNode_t* deps, size_t n_deps,
+                                   cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                                   cudaGraphNode_t* node, cudaGraph_t* body) {
   cudaGraphNodeParams np{};
   np.type = cudaGraphNodeTypeConditional;
   np.conditional.handle = h;
-  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.type = type;
   np.conditional.size = 1;
-  cudaGraphNode_t node;
-  e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
-  if (e != cudaSuccess) {
-    cudaGraphDestroy(g);
-    return check_launch(e, "cudaGraphAddNode(conditional)");
+  cudaError_t e = cudaGraphAddNode(node, g, deps, nullptr, n_deps, &np);
+  if (e == cudaSuccess) *body = np.conditional.phGraph_out[0];
+  return e;
+}
+
+// agb_solver_iterate's graph.  Without the reference-state correction:
+//   WHILE(c) { direction, gradient, vertex }   (the vertex pass sets c).
+// With it, the refresh passes run only when one is due:
+//   WHILE(outer) { WHILE(c) { direction, gradient, vertex }; refresh element, refresh vertex }
+// The vertex pass ends the inner loop when the solve ends, reaches the
+// iteration limit or asks for a refresh; the refresh vertex pass (which does
+// the refresh only if it was asked for) continues the outer loop and re-arms
+// the inner one unless the solve ended or reached the limit.
+static int build_loop_graph(agb_solver* sv) {
+  cudaGraph_t g = nullptr;
+  AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
+  const SolveArgs& a = sv->args;
+  cudaGraphConditionalHandle h_out = 0, h_in = 0;
+  cudaGraphNode_t w_out = nullptr, w_in = nullptr;
+  cudaGraph_t body_out = nullptr, body_in = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (a.delta) {
+    e = cudaGraphConditionalHandleCreate(&h_out, g, 1u, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = add_conditional(g, nullptr, 0, h_out, cudaGraphCondTypeWhile, &w_out, &body_out);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h_in, body_out, 1u, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = add_conditional(body_out, nullptr, 0, h_in, cudaGraphCondTypeWhile, &w_in, &body_in);
+    if (e == cudaSuccess) {
+      SolveArgs ai = a;
+      ai.cond = (unsigned long long)h_in;
+      ai.refresh_exits = 1;
+      e = capture_into(sv, body_in, nullptr, 0, ai, false);
+    }
+    if (e == cudaSuccess) {
+      SolveArgs ar = a;
+      ar.cond = (unsigned long long)h_in;
+      ar.cond_outer = (unsigned long long)h_out;
+      e = capture_into(sv, body_out, &w_in, 1, ar, true);
+    }
+  } else {
+    e = cudaGraphConditionalHandleCreate(&h_in, g, 1u, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = add_conditional(g, nullptr, 0, h_in, cudaGraphCondTypeWhile, &w_in, &body_in);
+    if (e == cudaSuccess) {
+      SolveArgs ai = a;
+      ai.cond = (unsigned long long)h_in;
+      e = capture_into(sv, body_in, nullptr, 0, ai, false);
+    }
   }
-  e = capture_iteration(sv, np.conditional.phGraph_out[0], (unsigned long long)h);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->loop_exec, g, 0);
   cudaGraphDestroy(g);
   return check_launch(e, "solver loop graph");
 }
 
+// agb_solver_step's graph: one iteration and, with the reference-state
+// correction, an IF node that runs the refresh passes when the vertex pass
+// asks for one.
 static int build_step_graph(agb_solver* sv) {
   cudaGraph_t g = nullptr;
   AGB_CHECK_CUDA(cudaGraphCreate(&g, 0));
-  cudaError_t e = capture_iteration(sv, g, 0ull);
+  SolveArgs a = sv->args;
+  cudaGraphConditionalHandle h_if = 0;
+  cudaError_t e = cudaSuccess;
+  if (a.delta) {
+    e = cudaGraphConditionalHandleCreate(&h_if, g, 0u, cudaGraphCondAssignDefault);
+    a.cond_refresh = (unsigned long long)h_if;
+  }
+  if (e == cudaSuccess) e = capture_into(sv, g, nullptr, 0, a, false);
   size_t n_nodes = 0;
   if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &n_nodes);
+  if (e == cudaSuccess && a.delta) {
+    std::vector<cudaGraphNode_t> leaves;
+    e = graph_leaves(g, &leaves);
+    cudaGraphNode_t w_if = nullptr;
+    cudaGraph_t body = nullptr;
+    if (e == cudaSuccess) e = add_conditional(g, leaves.data(), leaves.size(), h_if, cudaGraphCondTypeIf, &w_if, &body);
+    if (e == cudaSuccess) e = capture_into(sv, body, nullptr, 0, sv->args, true);
+  }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&sv->step_exec, g, 0);
   cudaGraphDestroy(g);
   sv->step_kernels = (int)n_nodes;
@@ -1062,6 +1129,40 @@ int agb_solver_read_direction(agb_solver* sv, void* p_host, void* stream) {
   unsigned char* out = static_cast<unsigned char*>(p_host);
   for (int i = 0; i < np; ++i)  // V4 (x, y, z, pad) at internal i -> 3 reals at caller uoi[i]
     std::memcpy(out + 3 * rb * (size_t)uoi[i], p4.data() + 4 * rb * (size_t)i, 3 * rb);
+  return AGB_OK;
+}
+
+int agb_solver_read_gradient(agb_solver* sv, void* g_host, void* d_host, void* stream) {
+  AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_read_gradient: null handle");
+  AGB_REQUIRE(sv->has_state, AGB_E_INVALID, "agb_solver_read_gradient: call agb_solver_reset first");
+  cudaStream_t s = as_stream(stream);
+  const int np = sv->args.n_points;
+  const size_t rb = real_bytes(sv->precision);
+  std::vector<unsigned char> gd(8 * rb * (size_t)np);  // per vertex: (g, 0), (d, 0)
+  AGB_CHECK_CUDA(cudaMemcpyAsync(gd.data(), sv->d_gd, gd.size(), cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  const std::vector<int32_t>& uoi = sv->model->space->user_of_internal;
+  unsigned char* go = static_cast<unsigned char*>(g_host);
+  unsigned char* dout = static_cast<unsigned char*>(d_host);
+  for (int i = 0; i < np; ++i) {
+    const size_t o = 3 * rb * (size_t)uoi[i];
+    if (go) std::memcpy(go + o, gd.data() + 8 * rb * (size_t)i, 3 * rb);
+    if (dout) std::memcpy(dout + o, gd.data() + 8 * rb * (size_t)i + 4 * rb, 3 * rb);
+  }
+  return AGB_OK;
+}
+
+int agb_solver_read_reductions(agb_solver* sv, double* out5, void* stream) {
+  AGB_REQUIRE(sv && out5, AGB_E_INVALID, "agb_solver_read_reductions: null argument");
+  cudaStream_t s = as_stream(stream);
+  AGB_CHECK_CUDA(cudaMemcpyAsync(sv->h_state, sv->d_state, sizeof(SolverState), cudaMemcpyDeviceToHost, s));
+  AGB_CHECK_CUDA(cudaStreamSynchronize(s));
+  const SolverState& st = *sv->h_state;
+  out5[0] = st.hq;
+  out5[1] = st.gd;
+  out5[2] = st.gnorm;
+  out5[3] = st.inv_mean;
+  out5[4] = st.beta;
   return AGB_OK;
 }
 

@@ -389,7 +389,12 @@ __device__ __forceinline__ void normalize3(R (&v)[3], R fallback_axis_seed) {
   }
 }
 
-template <class R>
+// With WARM, the Jacobi sweeps start from the rotation `out.V` holds on entry
+// (det +1): E is taken into that frame first, A = V0^T E V0, and the
+// rotations accumulate onto V0.  Near a point whose V0 is known (the ARAP
+// line-search trials around the base point), A is nearly diagonal and the
+// sweeps stop after one or two instead of four or five.
+template <class R, bool WARM = false>
 __device__ void svd_rv(const R (&G)[3][3], R jm1, Svd<R>& out) {
   R A[3][3];
 #pragma unroll
@@ -400,10 +405,22 @@ __device__ void svd_rv(const R (&G)[3][3], R jm1, Svd<R>& out) {
       A[i][j] = A[j][i] = G[i][j] + G[j][i] + gtg;
     }
   R (&V)[3][3] = out.V;
+  if constexpr (WARM) {
+    R EV[3][3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? R(1) : R(0);
+      for (int j = 0; j < 3; ++j) EV[i][j] = A[i][0] * V[0][j] + A[i][1] * V[1][j] + A[i][2] * V[2][j];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = i; j < 3; ++j) A[i][j] = A[j][i] = V[0][i] * EV[0][j] + V[1][i] * EV[1][j] + V[2][i] * EV[2][j];
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? R(1) : R(0);
+  }
   const R eps = sizeof(R) == 4 ? R(1e-7) : R(1e-15);
   for (int sweep = 0; sweep < 8; ++sweep) {
     const R off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];

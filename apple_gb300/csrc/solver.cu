@@ -193,7 +193,11 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
 #pragma unroll
         for (int k = 0; k < 3; ++k) Gt[i][k] = fma_rn(tj[j], dF[i][k], G[i][k]);
       Svd<R> trial;
-      svd_rv(Gt, (Gt[0][0] + Gt[1][1] + Gt[2][2]) + inv2(Gt) + det3(Gt), trial);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) trial.V[i][k] = base.V[i][k];
+      svd_rv<R, true>(Gt, (Gt[0][0] + Gt[1][1] + Gt[2][2]) + inv2(Gt) + det3(Gt), trial);
       sums[j].add(arap_remainder(base, trial, tj[j], dF, geo.mu));
     }
   }
@@ -257,8 +261,10 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
   pdl_wait();
   SolverState* st = a.st;
   if (st->done) {
-    if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
-      cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
+      if (a.cond_refresh) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_refresh, 0u);
+    }
     return;
   }
   const R t = (R)st->t;
@@ -285,9 +291,11 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
   if (!grid_reduce_masked<N, FF, R>(acc, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
   if (threadIdx.x != 0) return;
   vertex_decide(st, tot);
+  const bool go = !st->done && st->iter < st->iter_limit;
   if (use_cond)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
-                            (!st->done && st->iter < st->iter_limit) ? 1u : 0u);
+                            (go && !(a.refresh_exits && st->refresh)) ? 1u : 0u);
+  if (a.cond_refresh) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_refresh, st->refresh ? 1u : 0u);
 }
 
 // total energy at x, on demand: an element pass into per-tile partials, then
@@ -323,6 +331,14 @@ __global__ void __launch_bounds__(kGradThreads) solver_ref_elem_kernel(SolveArgs
 __global__ void __launch_bounds__(kVThreads) solver_ref_vertex_kernel(SolveArgs a) {
   pdl_trigger();
   pdl_wait();
+  if (a.cond_outer && blockIdx.x == 0 && threadIdx.x == 0) {
+    // after the inner loop of agb_solver_iterate: go on (and re-arm the inner
+    // loop) unless the solve ended or reached its iteration limit
+    const SolverState* st = a.st;
+    const bool go = !st->done && st->iter < st->iter_limit;
+    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_outer, go ? 1u : 0u);
+    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, go ? 1u : 0u);
+  }
   if (!a.st->refresh) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_points; i += gridDim.x * blockDim.x) ref_vertex(a, i);
 }
@@ -576,16 +592,20 @@ cudaError_t launch_solver_unpack_x(const SolveArgs& a, const void*, const int32_
   return cudaGetLastError();
 }
 
-cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s) {
+cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s, bool pdl) {
   if (!a.delta) return cudaSuccess;
   if (!a.xref || !a.gref || a.precision != AGB_F32 || !snh_family(a.fv.material)) return cudaErrorInvalidValue;
   const dim3 grid(ref_blocks(a.fv.n_tiles));
-  cudaError_t e = a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
-                      ? launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN_MUSCLE>, grid,
-                                   dim3(kGradThreads), ref_smem_bytes(), s, a)
-                      : launch_pdl(solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN>, grid,
-                                   dim3(kGradThreads), ref_smem_bytes(), s, a);
-  if (e == cudaSuccess) e = launch_pdl(solver_ref_vertex_kernel, dim3(a.vblocks), dim3(kVThreads), 0, s, a);
+  auto ek = a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE ? solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN_MUSCLE>
+                                                           : solver_ref_elem_kernel<AGB_STABLE_NEO_HOOKEAN>;
+  cudaError_t e = cudaSuccess;
+  if (pdl) {
+    e = launch_pdl(ek, grid, dim3(kGradThreads), ref_smem_bytes(), s, a);
+    if (e == cudaSuccess) e = launch_pdl(solver_ref_vertex_kernel, dim3(a.vblocks), dim3(kVThreads), 0, s, a);
+  } else {
+    ek<<<grid, kGradThreads, ref_smem_bytes(), s>>>(a);
+    solver_ref_vertex_kernel<<<a.vblocks, kVThreads, 0, s>>>(a);
+  }
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 

@@ -87,6 +87,15 @@ struct SolveArgs {
   int vblocks;
   int max_bt;               // Armijo halvings (ARAP trial passes launched)
   unsigned long long cond;  // cudaGraphConditionalHandle or 0
+  // Gating of the two reference-state refresh passes in the CUDA graphs:
+  // cond_refresh (an IF node around them, or 0) is set by the vertex pass to
+  // st->refresh; with refresh_exits the vertex pass also ends the WHILE loop
+  // `cond` when a refresh is due, and the refresh vertex pass, which follows
+  // that loop inside an outer WHILE loop `cond_outer`, re-arms `cond` and
+  // decides whether the outer loop continues.
+  unsigned long long cond_refresh;
+  unsigned long long cond_outer;
+  int refresh_exits;
 };
 
 cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,
@@ -109,8 +118,9 @@ size_t solver_grad_smem(int precision);
 // one pass of an iteration on its own: 0 direction, 1 gradient, 2 vertex
 cudaError_t launch_solver_pass(const SolveArgs& a, int which, cudaStream_t s);
 // the refresh of the reference state (element pass in FP64, vertex pass);
-// both return at once unless st->refresh is set
-cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s);
+// both return at once unless st->refresh is set.  pdl: launch them as
+// programmatic dependents of the kernel before them in the stream.
+cudaError_t launch_solver_refresh(const SolveArgs& a, cudaStream_t s, bool pdl = true);
 // set st->refresh (the next refresh passes run unconditionally)
 cudaError_t launch_solver_force_refresh(const SolveArgs& a, cudaStream_t s);
 

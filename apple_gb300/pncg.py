@@ -184,6 +184,23 @@ class DeviceSolver:
         _lib.call("agb_solver_read_direction", self.handle, ctypes.c_void_p(p.data_ptr()), stream_ptr())
         return p
 
+    def read_gradient(self) -> tuple[torch.Tensor, torch.Tensor]:
+        """The stored free gradient and clamped Hessian diagonal of the current
+        iterate (full (n_points, 3) CPU tensors of the model dtype, zero on
+        fixed DOFs)."""
+        n, dt = self.warp_model.n_points, self.warp_model.dtype
+        g = torch.empty((n, 3), dtype=dt)
+        d = torch.empty((n, 3), dtype=dt)
+        _lib.call("agb_solver_read_gradient", self.handle, ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(d.data_ptr()),
+                  stream_ptr())
+        return g, d
+
+    def read_reductions(self) -> dict:
+        """The FP64 scalars of the last iteration's global reductions."""
+        out = (ctypes.c_double * 5)()
+        _lib.call("agb_solver_read_reductions", self.handle, out, stream_ptr())
+        return {"hess_quad": out[0], "gd": out[1], "grad_norm": out[2], "precond_fill_inv": out[3], "beta": out[4]}
+
     def step_kernels(self) -> int:
         """Kernels one iteration launches (the nodes of the step graph)."""
         n = ctypes.c_int32()

@@ -238,13 +238,16 @@ int agb_solver_destroy(agb_solver* solver);
  * model's fixed values) and evaluate g_0, hess_diag_0. */
 int agb_solver_reset(agb_solver* solver, const void* u, void* stream);
 /* run up to n_steps iterations (fewer if the solve terminates); the loop
- * runs on the device as one CUDA graph launch (conditional while node). */
+ * runs on the device as one CUDA graph launch (conditional while node; with
+ * the FP32 correction on, the two refresh passes sit in an outer while loop
+ * and run only when a refresh is due). */
 int agb_solver_iterate(agb_solver* solver, int32_t n_steps, void* stream);
-/* exactly one iteration as a plain graph (benchmark building block) */
+/* exactly one iteration as one graph launch (benchmark building block); with
+ * the FP32 correction on, an IF node runs the two refresh passes when due */
 int agb_solver_step(agb_solver* solver, void* stream);
-/* number of kernels one iteration launches (the nodes of agb_solver_step's
- * graph: the three passes, plus the two reference-state refresh passes when
- * the FP32 correction is on) */
+/* number of kernels one iteration launches (the three passes of
+ * agb_solver_step's graph; the two refresh passes run in addition on the
+ * few iterations that refresh the FP32 correction's reference state) */
 int agb_solver_step_kernels(agb_solver* solver, int32_t* n_kernels);
 /* copy u out (device, caller order) and the stats (host); synchronises stream */
 int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
@@ -255,6 +258,19 @@ int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void
  * 20-ext-force-stable-neo-hookean-collision.py:211-224).  Synchronises the
  * stream; AGB_E_INVALID before the first agb_solver_reset / agb_solver_load. */
 int agb_solver_read_direction(agb_solver* solver, void* p_host, void* stream);
+/* The stored free gradient g and clamped Hessian diagonal d of the current
+ * iterate (zero on fixed components; PNCG state `grad` / `hess_diag`),
+ * copied to HOST memory in caller order, n_points x 3 of the solver
+ * precision each; either pointer may be NULL.  Synchronises the stream;
+ * AGB_E_INVALID before the first agb_solver_reset / agb_solver_load. */
+int agb_solver_read_gradient(agb_solver* solver, void* g_host, void* d_host, void* stream);
+/* The scalars the last iteration's reductions produced (FP64, from FP32
+ * per-thread sums and float-float trees in the FP32 build): out[0] = p^T H p
+ * of the last direction at its base point (the clamped per-element sum that
+ * sets alpha_0), out[1] = g . p_next = -g^T P g + beta p.g of the next
+ * direction, out[2] = ||g|| over the free DOFs, out[3] = the preconditioner's
+ * fill 1 / mean(|d| > 0), out[4] = beta.  Synchronises the stream. */
+int agb_solver_read_reductions(agb_solver* solver, double* out5, void* stream);
 
 /* Checkpoint / resume of a solve (the reference has none; its experiments
  * restart from saved .vtu states).  A checkpoint is the solver's whole PNCG
