@@ -61,6 +61,8 @@ def _args():
     ap.add_argument("--e2e-iters", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy record")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and adjoint sub-records")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
     ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular", "hbm-sizes", "muscle"],
                     default="plain",
@@ -112,6 +114,10 @@ class ClockSampler:
     NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
     def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        # one synchronous sample at the start, so that a timed region shorter
+        # than the sampling period still has a record
+        self.edges = self._sample_once()
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.p = subprocess.Popen(
@@ -120,21 +126,33 @@ class ClockSampler:
         except OSError:
             self.p = None
 
+    def _sample_once(self) -> list:
+        try:
+            r = subprocess.run(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                "-i", str(self.gpu)], capture_output=True, text=True, timeout=20)
+        except (OSError, subprocess.TimeoutExpired):
+            return []
+        return [row.split(",") for row in r.stdout.strip().splitlines() if row.count(",") >= 8]
+
     def stop(self) -> dict:
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
         self.p.wait(timeout=10)
         self.f.seek(0)
-        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        during = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
         os.unlink(self.f.name)
+        self.edges += self._sample_once()  # and one at the end
+        rows = during if during else self.edges
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
         reasons = sorted({n for r in rows for n, v in zip(self.NAMES, r[5:9]) if v.strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "source": "sampled every 100 ms during the timed region" if during
+                else "one sample at the start and one at the end (timed region shorter than the period)"}
 
 
 def _dist():
@@ -207,6 +225,309 @@ def cpu_reference(steps_req: int, budget: float, small: bool = False, warmup: in
                       f"atomic scatter; plus one trailing evaluation)"}
 
 
+def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100, rtol64=1e-8) -> dict:
+    """FP32 against FP64 on the headline workload, outside the timed region.
+
+    * energy and free gradient of the FP32 API path (``fun`` / ``grad`` of
+      the FP32 potential) against the FP64 C restatement of the reference
+      kernels, at the FP32 solver's iterate after ``n_mid`` iterations (the
+      gradient is still large there) and, for the energy, at the converged
+      FP32 answer u32;
+    * how converged u32 is in FP64: |g64(u32)| / |g64(u0)| on the free DOFs;
+    * the converged displacement against the FP64 build's solve to
+      ``rtol64`` (the FP64 kernels are pinned to the oracle at 1e-9):
+      max |u32 - u64| over the bounding-box diagonal.
+    """
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from oracle import build_c
+    from oracle import fem_oracle as O
+
+    dhdX, dV = O.region_compute_grad(m.points, m.cells)
+    cm = build_c.CModel(1, m.cells, dhdX, dV, mu, lam, m.n_points, mask=mask.astype(np.uint8))
+    free = ~mask
+
+    def c64(u):
+        r = cm.eval(np.asarray(u, np.float64), None, flags=3)
+        return r["fun"], r["grad"][free]
+
+    def gpu32(u):
+        U = torch.as_tensor(np.asarray(u, np.float32), device=dev)
+        e = torch.zeros(1, dtype=torch.float64, device=dev)
+        g = torch.zeros_like(U)
+        pot.fun(U, e)
+        pot.grad(U, g)
+        torch.cuda.synchronize(dev)
+        return float(e.item()), g.double().cpu().numpy()[free]
+
+    sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=n_mid, rtol=0.0)).solver(ag.ForwardProblem(model))
+    sv.reset(u0)
+    sv.iterate(n_mid)
+    u_mid = torch.empty_like(u0)
+    sv.read(u_mid)
+    um = u_mid.double().cpu().numpy()
+    e64m, g64m = c64(um)
+    e32m, g32m = gpu32(um)
+    uc = u32.double().cpu().numpy()
+    e64c, g64c = c64(uc)
+    e32c, _ = gpu32(uc)
+    _, g64_0 = c64(u0.double().cpu().numpy())
+    t0 = time.perf_counter()
+    sol64, u64 = _solve_f64(m, mu, lam, mask, fv, rtol64, dev)
+    t64 = time.perf_counter() - t0
+    diag = float(np.linalg.norm(m.points.max(0) - m.points.min(0)))
+    return {
+        "reference": "FP64 C restatement of the reference kernels (energy, gradient); the FP64 build's PNCG "
+                     f"to rtol {rtol64:g} (displacement)",
+        "energy_rel": abs(e32c - e64c) / abs(e64c),
+        "energy_rel_mid": abs(e32m - e64m) / abs(e64m),
+        "grad_rel_l2_mid": float(np.linalg.norm(g32m - g64m) / np.linalg.norm(g64m)),
+        "mid_iterate": n_mid,
+        "fp64_equilibrium_rel_grad": float(np.linalg.norm(g64c) / np.linalg.norm(g64_0)),
+        "disp_err_over_diag": float(np.abs(uc - u64.cpu().numpy()).max()) / diag,
+        "fp64_solve": {"result": sol64.result.name, "iters": sol64.n_steps, "seconds": t64,
+                       "rel_grad": sol64.grad_norm / sol64.grad_norm_first},
+        "bars": {"energy_rel": 1e-5, "grad_rel_l2": 1e-5, "disp_err_over_diag": 1e-4},
+    }
+
+
+def _solve_f64(m, mu, lam, mask, fv, rtol, dev, max_steps=20000):
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+
+    mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells), mu, lam)
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = fv
+    b = ag.ModelBuilder(dtype=torch.float64)
+    b.add_vertices(mesh)
+    b.add_fixed(mesh)
+    b.add_potential(ag.StableNeoHookean.from_pyvista(mesh, dtype=torch.float64))
+    model = b.finalize()
+    sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=max_steps, rtol=rtol)).solver(ag.ForwardProblem(model))
+    sv.reset(torch.tensor(np.where(mask, fv, 0.0), dtype=torch.float64, device=dev))
+    sv.iterate(max_steps)
+    u = torch.empty((m.n_points, 3), dtype=torch.float64, device=dev)
+    sol = sv.read(u)
+    return sol, u
+
+
+def loop_overhead_us(dev, n=2000) -> float:
+    """Microseconds per iteration of agb_solver_iterate's device loop on a
+    4x4x4-cell grid (320 tets), where the kernels have almost no work: the
+    fixed cost of an iteration's launches and grid-wide completions."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+
+    m = meshgen.grid(4, 4, 4)
+    lam, mu = meshgen.lame_converter(E_MOD, NU)
+    mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells), mu, lam)
+    mask = np.zeros((m.n_points, 3), bool)
+    mask[meshgen.face_mask(m, 2, "min")] = True
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = np.zeros((m.n_points, 3))
+    b = ag.ModelBuilder(dtype=torch.float32)
+    b.add_vertices(mesh)
+    b.add_fixed(mesh)
+    b.add_potential(ag.StableNeoHookean.from_pyvista(mesh))
+    fm = meshgen.TetMesh(m.points, m.cells)
+    fm.point_data["Force"] = meshgen.lumped_gravity(m, 1000.0)
+    fm.point_data["GlobalPointId"] = np.arange(m.n_points)
+    b.add_potential(ag.ExternalForce.from_pyvista(fm))
+    model = b.finalize()
+    sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=10**6, rtol=0.0)).solver(ag.ForwardProblem(model))
+    u0 = torch.zeros((m.n_points, 3), dtype=torch.float32, device=dev)
+    sv.reset(u0)
+    sv.iterate(3)
+    torch.cuda.synchronize(dev)
+    sv.reset(u0)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    sv.iterate(n)
+    st = sv.read()
+    dt = time.perf_counter() - t0
+    return 1e6 * dt / max(st.n_steps, 1)
+
+
+def batched_record(n=64, dims=(4, 40), max_steps=2000, rtol=1e-6, n_check=3, seed=0) -> dict:
+    """The batched form against the plain per-mesh form (a bounded sample of
+    the 512-mesh workload, outside the timed region): ``n`` uneven grids of
+    the batched workload's generator, each run to ``rtol`` or ``max_steps``
+    both ways.  A mesh in the batch runs exactly the single-mesh iteration
+    (its own beta, step and termination), so both forms reach the same
+    accuracy; the record checks that (max |u_batch - u_plain| / diagonal) and
+    measures both against FP64 solves of the C restatement of the reference
+    path on the ``n_check`` smallest meshes.  The reference steps one
+    ``Forward`` per model (forward/_forward.py:52-56)."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+    from apple_gb300.batch import BatchedForward
+    from oracle import build_c
+    from oracle import fem_oracle as O
+
+    rng = np.random.default_rng(seed)
+    cases = [meshgen.batch_case(k, rng, dims=dims, h=1.0 / 400) for k in range(n)]
+    crit = ag.ConvergenceCriteria(max_steps=max_steps, rtol=rtol)
+    models = _batch_models(cases, torch.float32)
+    bf = BatchedForward(models, ag.PNCG(crit))
+    n_points, n_cells = bf.info()
+    bf.solve(max_steps=3)  # graph capture
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bf.reset()
+    bf.iterate(max_steps)
+    sols, us = bf.read()
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    plain_u, plain_sols, t_plain = [], [], 0.0
+    for mdl in models:
+        opt = ag.PNCG(crit)
+        fwd = ag.Forward(mdl, opt)
+        opt.solver(fwd.problem)  # build and capture outside the timing, as for the batch
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        sol = fwd.step()
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t1
+        plain_sols.append(sol)
+        plain_u.append(fwd.state.u)
+    diag = [float(np.linalg.norm(m.points.max(0) - m.points.min(0))) for m, _ in cases]
+    d_bp = max(float((u.double() - v.double()).abs().max()) / d for u, v, d in zip(us, plain_u, diag))
+    err_b, err_p = [], []
+    for k in sorted(range(n), key=lambda k: cases[k][0].n_cells)[:n_check]:
+        m, f = cases[k]
+        dhdX, dV = O.region_compute_grad(m.points, m.cells)
+        cm = build_c.CModel(1, m.cells, dhdX, dV, m.cell_data["mu"], m.cell_data["lambda"], m.n_points,
+                            mask=np.asarray(m.point_data["FixedMask"], np.uint8), force=f)
+        u_ref, _ = cm.pncg(np.zeros((m.n_points, 3)), max_steps=50000, rtol=1e-10)
+        err_b.append(float(np.abs(us[k].double().cpu().numpy() - u_ref).max()) / diag[k])
+        err_p.append(float(np.abs(plain_u[k].double().cpu().numpy() - u_ref).max()) / diag[k])
+    iters = [s.n_steps for s in sols]
+    # the device loop's fixed cost per iteration (five kernels in a graph
+    # WHILE node): the same loop over two 4x4x4-cell grids, where the kernels
+    # have almost no work; a persistent kernel with grid barriers between the
+    # phases could save at most this much per iteration
+    tiny = [meshgen.batch_case(k, np.random.default_rng(99), dims=(4, 4), h=1.0 / 400) for k in range(2)]
+    tb = BatchedForward(_batch_models(tiny, torch.float32),
+                        ag.PNCG(ag.ConvergenceCriteria(max_steps=10**6, rtol=0.0)))
+    tb.solve(max_steps=3)
+    torch.cuda.synchronize()
+    tb.reset()
+    t0 = time.perf_counter()
+    tb.iterate(2000)
+    tsols, _ = tb.read(with_u=False)
+    torch.cuda.synchronize()
+    t_tiny = time.perf_counter() - t0
+    return {
+        "workload": f"{n} grids of the batched workload's generator, {dims[0]}-{dims[1]} cells per axis "
+                    f"(seed {seed}), FP32, rtol {rtol:g} or {max_steps} iterations",
+        "n_meshes": n, "n_tets": n_cells, "n_vertices": n_points,
+        "batched_s": t_batch, "plain_s": t_plain, "speedup": t_plain / t_batch,
+        "iters_total": int(sum(iters)), "iters_equal": all(s.n_steps == p.n_steps for s, p in zip(sols, plain_sols)),
+        "converged": {"batched": int(sum(s.result == ag.Result.PRIMARY_SUCCESS for s in sols)),
+                      "plain": int(sum(s.result == ag.Result.PRIMARY_SUCCESS for s in plain_sols))},
+        "max_diff_batched_vs_plain_over_diag": d_bp,
+        "fp64_reference_err_over_diag": {"meshes": n_check, "batched": max(err_b), "plain": max(err_p),
+                                         "reference": "FP64 C restatement of the reference PNCG, rtol 1e-10"},
+        "loop_us_per_iter": {"this_batch": 1e6 * t_batch / max(iters),
+                             "two_4x4x4_grids": 1e6 * t_tiny / max(max(s.n_steps for s in tsols), 1)},
+    }
+
+
+def adjoint_record(small=False, seed=0) -> dict:
+    """The adjoint form against the plain forward (the 24x24x48-cell adjoint
+    workload, 138,240 tets, one theta per tet scaling mu; outside the timed
+    region): one forward solve (FP32, rtol 1e-7) plus the device adjoint (CG
+    with H p, then the material VJP) gives all 138,240 derivatives, where
+    the plain form needs two forward solves per parameter.  Accuracy: the
+    directional derivative along a random direction against central
+    differences of two FP64 forwards (started from u*, stopped at 1e-12 of
+    the cold-start gradient), and FP32 vs FP64 adjoint.  The reference's
+    recipe: exp/2025/09/24/inverse-grin/src/32-inverse.py:223-260."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+    from apple_gb300.adjoint import MaterialEquilibrium
+
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = (6, 6, 12) if small else (24, 24, 48)
+    m = meshgen.grid(nx, ny, nz, h=1.0 / nx)
+    lam0, mu0 = meshgen.lame_converter(E_MOD, NU)
+    theta = rng.uniform(0.5, 2.0, m.n_cells)
+    theta_star = rng.uniform(0.5, 2.0, m.n_cells)
+    mask = np.zeros((m.n_points, 3), bool)
+    fv = np.zeros((m.n_points, 3))
+    mask[meshgen.face_mask(m, 2, "min")] = True
+    top = meshgen.face_mask(m, 2, "max")
+    mask[top] = True
+    fv[top, 2] = STRETCH * m.points[:, 2].max()
+    surf = np.zeros(m.n_points, bool)
+    for ax in range(3):
+        for side in ("min", "max"):
+            surf |= meshgen.face_mask(m, ax, side)
+    mesh = meshgen.TetMesh(m.points, m.cells)
+    mesh.point_data["FixedMask"] = mask
+    mesh.point_data["FixedValue"] = fv
+    lam = lam0 * np.ones(m.n_cells)
+    p32 = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float32,
+                              criteria=ag.ConvergenceCriteria(max_steps=200000, rtol=1e-7), cg_rtol=1e-6)
+    p64 = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float64,
+                              criteria=ag.ConvergenceCriteria(max_steps=200000, rtol=1e-10), cg_rtol=1e-10)
+    dev = torch.device("cuda")
+    si = torch.tensor(np.flatnonzero(surf), device=dev)
+    target = p64.solve(mu0 * theta_star, lam)[si].clone()
+
+    def loss(u):
+        return 0.5 * float(((u.double()[si] - target) ** 2).sum())
+
+    def gradient(prob, th):
+        u = prob.solve(mu0 * th, lam)
+        g = torch.zeros_like(u)
+        g[si] = (u.double()[si] - target).to(u.dtype)
+        d = prob.vjp(g)["mu"].double().cpu().numpy() * mu0
+        return loss(u), d, dict(prob.timings), prob.stats
+
+    gradient(p32, theta)  # warm-up: graph capture, kernel attributes
+    _, d32, t32, s32 = gradient(p32, theta)
+    _, d64, _, s64 = gradient(p64, theta)
+    g_first = s64.forward.grad_norm_first
+    p_fd = MaterialEquilibrium(mesh, ag.StableNeoHookean, dtype=torch.float64,
+                               criteria=ag.ConvergenceCriteria(max_steps=400000, rtol=0.0, atol=1e-12 * g_first))
+    u_base = p_fd.solve(mu0 * theta, lam, u0=p64.solve(mu0 * theta, lam)).clone()
+    v = rng.normal(size=m.n_cells)
+    hd = 1e-2
+    lp = loss(p_fd.solve(mu0 * theta * (1.0 + hd * v), lam, u0=u_base))
+    lm = loss(p_fd.solve(mu0 * theta * (1.0 - hd * v), lam, u0=u_base))
+    fd_dir = (lp - lm) / (2 * hd)
+    dir32, dir64 = float(np.dot(d32, v * theta)), float(np.dot(d64, v * theta))
+    fwd32, adj32 = t32["forward"], t32["adjoint"]
+    return {
+        "workload": ADJ_WORKLOAD if not small else "snh_grid_6x6x12_adjoint",
+        "n_tets": m.n_cells, "n_params": m.n_cells,
+        "forward_s": fwd32, "forward_iters": s32.forward.n_steps, "adjoint_s": adj32, "cg_iters": s32.cg.n_iter,
+        "gradient_s": fwd32 + adj32,
+        "plain_s_est": 2 * m.n_cells * fwd32,
+        "plain": "central differences of the plain forward: 2 solves per parameter",
+        "speedup_est": 2 * m.n_cells * fwd32 / (fwd32 + adj32),
+        "adjoint_over_one_forward": adj32 / fwd32,
+        "directional_rel_err_vs_fd": {"f32": abs(dir32 - fd_dir) / abs(fd_dir),
+                                      "f64": abs(dir64 - fd_dir) / abs(fd_dir)},
+        "f32_vs_f64_adjoint_rel": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
+    }
+
+
 def run_reference(a) -> None:
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -242,7 +563,8 @@ def run_ours(a) -> None:
     mesh.point_data["FixedMask"] = mask
     mesh.point_data["FixedValue"] = fv
     b.add_fixed(mesh)
-    b.add_potential(ag.StableNeoHookean.from_pyvista(mesh))
+    pot = ag.StableNeoHookean.from_pyvista(mesh)
+    b.add_potential(pot)
     model = b.finalize()
     nt, nv = m.n_cells, m.n_points
     u0 = torch.tensor(np.where(mask, fv, 0.0), dtype=torch.float32, device=dev)
@@ -321,10 +643,27 @@ def run_ours(a) -> None:
     t0 = time.perf_counter()
     solve_sv.reset(u0)
     solve_sv.iterate(20000)
-    ssol = solve_sv.read()
+    u32 = torch.empty_like(u0)
+    ssol = solve_sv.read(u32)
     t_solve = time.perf_counter() - t0
     solve = {"rtol": 1e-6, "result": ssol.result.name, "iters": ssol.n_steps, "seconds": t_solve,
              "rel_grad": ssol.grad_norm / ssol.grad_norm_first, "iters_per_s": ssol.n_steps / t_solve}
+    loop_us = loop_overhead_us(dev)
+    accuracy = batched = adjoint = None
+    if rank == 0 and not a.no_accuracy:
+        try:
+            accuracy = headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev)
+        except Exception as e:  # noqa: BLE001
+            accuracy = {"failed": f"{type(e).__name__}: {e}"}
+    if rank == 0 and not a.no_forms:
+        try:
+            batched = batched_record(n=16 if a.small else 64)
+        except Exception as e:  # noqa: BLE001
+            batched = {"failed": f"{type(e).__name__}: {e}"}
+        try:
+            adjoint = adjoint_record(small=a.small)
+        except Exception as e:  # noqa: BLE001
+            adjoint = {"failed": f"{type(e).__name__}: {e}"}
 
     # end to end through the public host-buffer API
     e2e_opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=a.e2e_iters, rtol=0.0))
@@ -372,6 +711,10 @@ def run_ours(a) -> None:
             "passes_ms": {n: ms[i] for i, n in enumerate(names)},
             "e2e": e2e,
             "solve_to_1e-6": solve,
+            "loop_us_per_iter_320_tets": loop_us,
+            "accuracy": accuracy,
+            "batched": batched,
+            "adjoint": adjoint,
             "cpu_baseline": cpu,
             "gpu_launches": solver.step_kernels() * a.steps,
             "clocks": clk,
