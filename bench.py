@@ -64,7 +64,8 @@ def _args():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy record")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and adjoint sub-records")
     ap.add_argument("--small", action="store_true", help="16x16x40 grid (smoke / profiling runs)")
-    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular", "hbm-sizes", "muscle"],
+    ap.add_argument("--config", choices=["plain", "adjoint", "batched", "grid64", "irregular", "irregular-study",
+                                         "hbm-sizes", "muscle"],
                     default="plain",
                     help="plain: the headline PNCG line; adjoint: the 138k-tet adjoint workload; "
                          "batched: 512 uneven meshes in one batch vs solved one by one; grid64: the "
@@ -1176,6 +1177,72 @@ def run_irregular(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_irregular_study(a) -> None:
+    """Why the irregular workload converges slowly: the same Delaunay ball at a
+    smaller size (20,000 + 3,000 points, the small irregular workload) solved
+    by Jacobi-preconditioned PNCG in FP32 and FP64 on the GPU and by the FP64
+    C restatement of the reference's PNCG on the host, with the workload's
+    stiffness contrast (mu log-uniform over three decades) and with a uniform
+    mu (the contrast's geometric mean).  ||g|| / ||g0|| is recorded at fixed
+    iteration counts."""
+    import numpy as np
+    import torch
+
+    import apple_gb300 as ag
+    from apple_gb300 import meshgen
+    from oracle import build_c
+    from oracle import fem_oracle as O
+
+    m = meshgen.ball(20000, 3000, seed=0)
+    rng = np.random.default_rng(0)
+    pts, cells = m.points, np.asarray(m.cells, np.int32)
+    mask = np.zeros((pts.shape[0], 3), bool)
+    mask[pts[:, 2] < -0.9] = True
+    f = meshgen.lumped_gravity(m, 1000.0)
+    dev = torch.device("cuda")
+    marks = (1000, 5000, 20000)
+    c_marks = (1000, 5000)
+    out = {"workload": "snh_delaunay_ball_small (20,000 + 3,000 points), gravity, cap z < -0.9 fixed",
+           "n_tets": int(cells.shape[0]), "n_vertices": int(pts.shape[0]), "rel_grad_at": {}}
+    mu_contrast = np.exp(rng.uniform(np.log(1e3), np.log(1e6), cells.shape[0]))
+    for name, mu in (("mu_log_uniform_1e3_1e6", mu_contrast),
+                     ("mu_uniform_geometric_mean", np.full(cells.shape[0], np.sqrt(1e3 * 1e6)))):
+        rec = {}
+        mesh = meshgen.TetMesh(pts, cells)
+        mesh.cell_data["mu"] = mu
+        mesh.cell_data["lambda"] = 10.0 * mu
+        mesh.point_data["FixedMask"] = mask
+        mesh.point_data["FixedValue"] = np.zeros((pts.shape[0], 3))
+        for dt in (torch.float32, torch.float64):
+            b = ag.ModelBuilder(dtype=dt)
+            b.add_vertices(mesh)
+            b.add_fixed(mesh)
+            b.add_potential(ag.StableNeoHookean.from_pyvista(mesh, dtype=dt))
+            fm = meshgen.TetMesh(pts, cells)
+            fm.point_data["Force"] = f
+            fm.point_data["GlobalPointId"] = np.arange(pts.shape[0])
+            b.add_potential(ag.ExternalForce.from_pyvista(fm, dtype=dt))
+            sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=10**6, rtol=0.0)).solver(ag.ForwardProblem(b.finalize()))
+            sv.reset(torch.zeros((pts.shape[0], 3), dtype=dt, device=dev))
+            done, traj = 0, {}
+            for k in marks:
+                sv.iterate(k - done)
+                done = k
+                st = sv.read()
+                traj[k] = {"rel_grad": st.grad_norm / st.grad_norm_first, "result": st.result.name,
+                           "iters": st.n_steps}
+            rec["gpu_" + ("f32" if dt == torch.float32 else "f64")] = traj
+        dhdX, dV = O.region_compute_grad(pts, cells)
+        cm = build_c.CModel(1, cells, dhdX, dV, mu, 10.0 * mu, pts.shape[0], mask=mask.astype(np.uint8), force=f)
+        traj = {}
+        for k in c_marks:
+            _, st = cm.pncg(np.zeros((pts.shape[0], 3)), max_steps=k, rtol=0.0)
+            traj[k] = {"rel_grad": st.grad_norm / st.grad_norm_first, "iters": int(st.n_steps)}
+        rec["c_restatement_f64"] = traj
+        out["rel_grad_at"][name] = rec
+    print(json.dumps(out), flush=True)
+
+
 def run_muscle(a) -> None:
     """The headline grid (stretch 30%) as a stable Neo-Hookean muscle with a
     random per-cell activation (|a| ~ 0.05) vs the same grid without it:
@@ -1273,6 +1340,8 @@ def main():
         run_hbm_sizes(a)
     elif a.config == "muscle":
         run_muscle(a)
+    elif a.config == "irregular-study":
+        run_irregular_study(a)
     elif a.config == "irregular":
         run_irregular(a)
     else:

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _column():
-    m = meshgen.grid(6, 5, 12)
+    m = meshgen.grid(10, 10, 10)
     lam, mu = meshgen.lame_converter(1e4, 0.45)
     mesh = ag.with_lame(meshgen.TetMesh(m.points, m.cells), mu, lam)
     mask = np.zeros((m.n_points, 3), bool)
@@ -36,23 +36,21 @@ def _column():
 
 def test_loop_chunks_and_steps_agree_bitwise(cuda_device):
     model = _column()
-    n = 400
+    n = 500
     u0 = ag.Forward(model, ag.PNCG()).state.u
     runs = {}
     for mode in ("loop", "chunks", "steps"):
-        # rtol 0 keeps every run going for exactly n iterations; the
-        # correction (refresh each 100x drop of ||g||) is asked for explicitly
+        # rtol 0: every run goes on until n iterations or until the line
+        # search cannot decrease the energy any more; the correction (refresh
+        # each 100x drop of ||g||) is asked for explicitly
         opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=10**6, rtol=0.0), refresh_ratio=1e-2)
         sv = opt.solver(ag.ForwardProblem(model))
         sv.reset(u0)
         if mode == "loop":
             sv.iterate(n)
         elif mode == "chunks":
-            done = 0
-            for c in (1, 7, 50, 3, 139, 200):
+            for c in (1, 7, 50, 3, 139, 300):
                 sv.iterate(c)
-                done += c
-            assert done == n
         else:
             for _ in range(n):
                 sv.step()
@@ -61,12 +59,13 @@ def test_loop_chunks_and_steps_agree_bitwise(cuda_device):
         g, d = sv.read_gradient()
         runs[mode] = (u.cpu(), g, d, st)
     u, g, d, st = runs["loop"]
-    assert st.n_steps == n
+    assert st.n_steps > 100
     # far enough down for several refreshes (one per 100x drop of ||g||)
-    assert st.grad_norm / st.grad_norm_first < 1e-4
+    assert st.grad_norm / st.grad_norm_first < 1e-5, st
     for mode in ("chunks", "steps"):
         u2, g2, d2, st2 = runs[mode]
-        assert st2.n_steps == n
+        assert st2.n_steps == st.n_steps, mode
+        assert st2.result == st.result, mode
         assert torch.equal(u, u2), mode
         assert torch.equal(g, g2), mode
         assert torch.equal(d, d2), mode
