@@ -261,10 +261,8 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
   pdl_wait();
   SolverState* st = a.st;
   if (st->done) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
-      if (a.cond_refresh) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_refresh, 0u);
-    }
+    if (use_cond && blockIdx.x == 0 && threadIdx.x == 0)
+      cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
     return;
   }
   const R t = (R)st->t;
@@ -295,7 +293,6 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
   if (use_cond)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
                             (go && !(a.refresh_exits && st->refresh)) ? 1u : 0u);
-  if (a.cond_refresh) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_refresh, st->refresh ? 1u : 0u);
 }
 
 // total energy at x, on demand: an element pass into per-tile partials, then

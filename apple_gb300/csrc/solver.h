@@ -87,13 +87,11 @@ struct SolveArgs {
   int vblocks;
   int max_bt;               // Armijo halvings (ARAP trial passes launched)
   unsigned long long cond;  // cudaGraphConditionalHandle or 0
-  // Gating of the two reference-state refresh passes in the CUDA graphs:
-  // cond_refresh (an IF node around them, or 0) is set by the vertex pass to
-  // st->refresh; with refresh_exits the vertex pass also ends the WHILE loop
-  // `cond` when a refresh is due, and the refresh vertex pass, which follows
-  // that loop inside an outer WHILE loop `cond_outer`, re-arms `cond` and
-  // decides whether the outer loop continues.
-  unsigned long long cond_refresh;
+  // Gating of the two reference-state refresh passes in agb_solver_iterate's
+  // graph: with refresh_exits the vertex pass also ends the WHILE loop `cond`
+  // when a refresh is due, and the refresh vertex pass, which follows that
+  // loop inside an outer WHILE loop `cond_outer`, re-arms `cond` and decides
+  // whether the outer loop continues.
   unsigned long long cond_outer;
   int refresh_exits;
 };

@@ -226,18 +226,23 @@ def cpu_reference(steps_req: int, budget: float, small: bool = False, warmup: in
                       f"atomic scatter; plus one trailing evaluation)"}
 
 
-def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100, rtol64=1e-8) -> dict:
+def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100, rtol_tight=1e-8,
+                      rtol64=1e-10) -> dict:
     """FP32 against FP64 on the headline workload, outside the timed region.
 
-    * energy and free gradient of the FP32 API path (``fun`` / ``grad`` of
-      the FP32 potential) against the FP64 C restatement of the reference
-      kernels, at the FP32 solver's iterate after ``n_mid`` iterations (the
-      gradient is still large there) and, for the energy, at the converged
-      FP32 answer u32;
-    * how converged u32 is in FP64: |g64(u32)| / |g64(u0)| on the free DOFs;
-    * the converged displacement against the FP64 build's solve to
-      ``rtol64`` (the FP64 kernels are pinned to the oracle at 1e-9):
-      max |u32 - u64| over the bounding-box diagonal.
+    * energy and free gradient against the FP64 C restatement of the
+      reference kernels: of the FP32 API path (``fun`` / ``grad`` of the FP32
+      potential) at the initial state and at the FP32 solver's iterate after
+      ``n_mid`` iterations, and of the solver's own stored gradient (the
+      reference-state correction) at that iterate;
+    * how converged the headline's FP32 answer u32 (rtol 1e-6) is in FP64:
+      |g64(u32)| / |g64(u0)| on the free DOFs;
+    * displacements against the FP64 build's solve to ``rtol64`` (the FP64
+      kernels are pinned to the oracle at 1e-9): the FP32 solve to
+      ``rtol_tight`` (FP32 arithmetic at matched, tight tolerance), and u32
+      (which adds the tolerance's own error: at nu = 0.49 and 30% stretch
+      the equilibrium is ill-conditioned, so ||g||/||g0|| = 1e-6 leaves a
+      displacement error of order 1% of the diagonal in any precision).
     """
     import numpy as np
     import torch
@@ -263,38 +268,53 @@ def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100,
         torch.cuda.synchronize(dev)
         return float(e.item()), g.double().cpu().numpy()[free]
 
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+    u0h = u0.double().cpu().numpy()
+    e64_0, g64_0 = c64(u0h)
+    e32_0, g32_0 = gpu32(u0h)
     sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=n_mid, rtol=0.0)).solver(ag.ForwardProblem(model))
     sv.reset(u0)
     sv.iterate(n_mid)
     u_mid = torch.empty_like(u0)
     sv.read(u_mid)
+    gs, _ = sv.read_gradient()
     um = u_mid.double().cpu().numpy()
     e64m, g64m = c64(um)
     e32m, g32m = gpu32(um)
     uc = u32.double().cpu().numpy()
     e64c, g64c = c64(uc)
     e32c, _ = gpu32(uc)
-    _, g64_0 = c64(u0.double().cpu().numpy())
+    tight = ag.PNCG(ag.ConvergenceCriteria(max_steps=40000, rtol=rtol_tight)).solver(ag.ForwardProblem(model))
+    tight.reset(u0)
+    tight.iterate(40000)
+    ut = torch.empty_like(u0)
+    st_t = tight.read(ut)
     t0 = time.perf_counter()
     sol64, u64 = _solve_f64(m, mu, lam, mask, fv, rtol64, dev)
     t64 = time.perf_counter() - t0
+    u64h = u64.cpu().numpy()
     diag = float(np.linalg.norm(m.points.max(0) - m.points.min(0)))
     return {
         "reference": "FP64 C restatement of the reference kernels (energy, gradient); the FP64 build's PNCG "
                      f"to rtol {rtol64:g} (displacement)",
-        "energy_rel": abs(e32c - e64c) / abs(e64c),
-        "energy_rel_mid": abs(e32m - e64m) / abs(e64m),
-        "grad_rel_l2_mid": float(np.linalg.norm(g32m - g64m) / np.linalg.norm(g64m)),
-        "mid_iterate": n_mid,
-        "fp64_equilibrium_rel_grad": float(np.linalg.norm(g64c) / np.linalg.norm(g64_0)),
-        "disp_err_over_diag": float(np.abs(uc - u64.cpu().numpy()).max()) / diag,
+        "energy_rel": {"u0": abs(e32_0 - e64_0) / abs(e64_0), f"iterate_{n_mid}": abs(e32m - e64m) / abs(e64m),
+                       "u32": abs(e32c - e64c) / abs(e64c)},
+        "grad_rel_l2": {"u0_api": rel(g32_0, g64_0), f"iterate_{n_mid}_api": rel(g32m, g64m),
+                        f"iterate_{n_mid}_solver": rel(gs.double().numpy()[free], g64m)},
+        "fp64_rel_grad_of_u32": float(np.linalg.norm(g64c) / np.linalg.norm(g64_0)),
+        "disp_err_over_diag": {f"f32_rtol_{rtol_tight:g}": float(np.abs(ut.double().cpu().numpy() - u64h).max()) / diag,
+                               "u32_rtol_1e-06": float(np.abs(uc - u64h).max()) / diag},
+        "f32_tight_solve": {"result": st_t.result.name, "iters": st_t.n_steps,
+                            "rel_grad": st_t.grad_norm / st_t.grad_norm_first},
         "fp64_solve": {"result": sol64.result.name, "iters": sol64.n_steps, "seconds": t64,
                        "rel_grad": sol64.grad_norm / sol64.grad_norm_first},
         "bars": {"energy_rel": 1e-5, "grad_rel_l2": 1e-5, "disp_err_over_diag": 1e-4},
     }
 
 
-def _solve_f64(m, mu, lam, mask, fv, rtol, dev, max_steps=20000):
+def _solve_f64(m, mu, lam, mask, fv, rtol, dev, max_steps=40000):
     import numpy as np
     import torch
 

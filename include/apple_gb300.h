@@ -243,11 +243,11 @@ int agb_solver_reset(agb_solver* solver, const void* u, void* stream);
  * and run only when a refresh is due). */
 int agb_solver_iterate(agb_solver* solver, int32_t n_steps, void* stream);
 /* exactly one iteration as one graph launch (benchmark building block); with
- * the FP32 correction on, an IF node runs the two refresh passes when due */
+ * the FP32 correction on, the two refresh passes follow and return at once
+ * unless a refresh is due */
 int agb_solver_step(agb_solver* solver, void* stream);
-/* number of kernels one iteration launches (the three passes of
- * agb_solver_step's graph; the two refresh passes run in addition on the
- * few iterations that refresh the FP32 correction's reference state) */
+/* number of kernels one iteration of agb_solver_step launches (the three
+ * passes, plus the two refresh passes when the FP32 correction is on) */
 int agb_solver_step_kernels(agb_solver* solver, int32_t* n_kernels);
 /* copy u out (device, caller order) and the stats (host); synchronises stream */
 int agb_solver_read(agb_solver* solver, void* u_out, agb_pncg_stats* stats, void* stream);
