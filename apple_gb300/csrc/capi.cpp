@@ -917,6 +917,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.cond = 0;
   a.cond_outer = 0;
   a.refresh_exits = 0;
+  a.guard = 0;
   *out = sv;
   return AGB_OK;
 }
@@ -939,12 +940,25 @@ int agb_solver_reset(agb_solver* sv, const void* u, void* stream) {
 // Capture into `graph` after `deps` (which may be empty): the three passes
 // of one iteration (refresh = false) or the two refresh passes as plain
 // launches (refresh = true).
+// Iterations per body of agb_solver_iterate's WHILE loop: the second of two
+// is guarded (its passes return at once when the first ended the run), its
+// direction pass a programmatic dependent of the first's vertex pass, and
+// the loop's condition is evaluated once per two iterations.
+#ifndef AGB_LOOP_UNROLL
+#define AGB_LOOP_UNROLL 2
+#endif
+
 static cudaError_t capture_into(agb_solver* sv, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t n_deps,
                                 const SolveArgs& a, bool refresh) {
   cudaStream_t cs = sv->capture_stream;
   cudaError_t e = cudaStreamBeginCaptureToGraph(cs, graph, deps, nullptr, n_deps, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
   cudaError_t le = refresh ? launch_solver_refresh(a, cs, false) : launch_solver_iteration(a, a.cond != 0, cs);
+  for (int k = 1; !refresh && le == cudaSuccess && k < AGB_LOOP_UNROLL; ++k) {
+    SolveArgs ag = a;
+    ag.guard = 1;
+    le = launch_solver_iteration(ag, ag.cond != 0, cs);
+  }
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(cs, &captured);
   return e == cudaSuccess ? le : e;

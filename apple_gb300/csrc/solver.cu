@@ -61,10 +61,6 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   __shared__ Acc<R> red[kWarps * N];
   SolverState* st = a.st;
   pdl_trigger();
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
-    st->refresh = 0;  // the refresh passes, if any, ran after the last vertex pass
-  }
   static_assert(kTileVerts == kElemThreads, "one staged vertex per thread");
   int tile = blockIdx.x;
   // constant inputs first: the thread's first element record and vertex id
@@ -74,7 +70,14 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   uint32_t ids = 0;
   if (e < ee) load_elem_m<R, MAT>(a.fv, e, geo, ids);
   int vid = tile_vertex(a.fv, tile, threadIdx.x);
-  if (st->done) return;
+  pdl_wait();  // launched as a dependent of the vertex pass in an unrolled loop body
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);  // vertex pass re-arms
+    // the refresh passes, if any, ran after the last vertex pass (a guarded
+    // pass that goes on finds no refresh pending)
+    if (!a.guard) st->refresh = 0;
+  }
+  if (st->done || guard_skip(a, st)) return;
   const R beta = (R)st->beta, inv_mean = (R)st->inv_mean;
   const int pb = st->pbuf;
   const V4<R>* pprev = p_prev<R>(a, pb);
@@ -265,6 +268,7 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
       cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
     return;
   }
+  if (guard_skip(a, st)) return;  // the loop condition stays as the direction pass left it: 0
   const R t = (R)st->t;
   const V4<R>* P = p_cur<R>(a, st->pbuf);
   // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
@@ -495,7 +499,15 @@ static cudaError_t launch_iteration_d(const SolveArgs& a, bool use_cond, bool fi
                                       cudaStream_t s) {
   const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
   if (!first) {
-    solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, use_cond ? 1 : 0);
+    // a guarded iteration follows another one: its direction pass is a
+    // programmatic dependent of that iteration's vertex pass
+    if (a.guard) {
+      cudaError_t e = launch_pdl(solver_dir_kernel<R, MAT>, dim3(dir_blocks(a.fv.n_tiles)), eb, 0, s, a,
+                                 use_cond ? 1 : 0);
+      if (e != cudaSuccess) return e;
+    } else {
+      solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, use_cond ? 1 : 0);
+    }
     if constexpr (MAT == AGB_ARAP) {
       for (int j0 = 0; j0 <= max_bt; j0 += 3) solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0);
     }

@@ -94,6 +94,10 @@ struct SolveArgs {
   // whether the outer loop continues.
   unsigned long long cond_outer;
   int refresh_exits;
+  // second iteration of an unrolled loop body: its passes return at once
+  // (with no effect) when the first one ended the solve, reached the
+  // iteration limit or asked for a refresh
+  int guard;
 };
 
 cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,

@@ -21,6 +21,12 @@ constexpr int kGradWarps = kGradThreads / 32;
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// the passes of a guarded iteration (SolveArgs::guard) skip it when the one
+// before it ended the solve's run: limit reached or refresh due
+__device__ __forceinline__ bool guard_skip(const SolveArgs& a, const SolverState* st) {
+  return a.guard && (st->iter >= st->iter_limit || st->refresh);
+}
+
 __device__ __forceinline__ double initial_alpha(double gd, double hq, double overstep) {
   double a = -gd / hq;
   if (isnan(a)) a = 0.0;
@@ -473,7 +479,7 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
   }
   pdl_trigger();
   pdl_wait();
-  if (st->done) return;
+  if (st->done || guard_skip(a, st)) return;
   if constexpr (DELTA)
     stage_point_delta<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
   else
