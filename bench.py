@@ -296,6 +296,26 @@ def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100,
     t64 = time.perf_counter() - t0
     u64h = u64.cpu().numpy()
     diag = float(np.linalg.norm(m.points.max(0) - m.points.min(0)))
+    # two equilibria or one?  each precision restarted from the other's answer
+    uth = ut.double().cpu().numpy()
+    sol64b, u64b = _solve_f64(m, mu, lam, mask, fv, rtol64, dev, u_init=ut.double())
+    back = ag.PNCG(ag.ConvergenceCriteria(max_steps=40000, rtol=rtol_tight)).solver(ag.ForwardProblem(model))
+    back.reset(u64.float())
+    back.iterate(40000)
+    u32b = torch.empty_like(u0)
+    back.read(u32b)
+    e_t, _ = c64(uth)
+    e_64, g_64 = c64(u64h)
+    e_64b, _ = c64(u64b.cpu().numpy())
+    restarts = {
+        "fp64_energy": {f"at_f32_rtol_{rtol_tight:g}": e_t, "at_fp64": e_64, "at_fp64_from_f32": e_64b},
+        "fp64_from_f32_answer": {"iters": sol64b.n_steps, "rel_grad": sol64b.grad_norm / sol64b.grad_norm_first,
+                                 "moved_over_diag": float(np.abs(u64b.cpu().numpy() - uth).max()) / diag,
+                                 "to_fp64_answer_over_diag": float(np.abs(u64b.cpu().numpy() - u64h).max()) / diag},
+        "f32_from_fp64_answer_over_diag": float(np.abs(u32b.double().cpu().numpy() - u64h).max()) / diag,
+        "rel_diff_over_diag_quantiles_f32_vs_fp64": np.quantile(np.abs(uth - u64h).max(axis=1) / diag,
+                                                                  [0.5, 0.9, 0.99, 1.0]).tolist(),
+    }
     return {
         "reference": "FP64 C restatement of the reference kernels (energy, gradient); the FP64 build's PNCG "
                      f"to rtol {rtol64:g} (displacement)",
@@ -306,6 +326,7 @@ def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100,
         "fp64_rel_grad_of_u32": float(np.linalg.norm(g64c) / np.linalg.norm(g64_0)),
         "disp_err_over_diag": {f"f32_rtol_{rtol_tight:g}": float(np.abs(ut.double().cpu().numpy() - u64h).max()) / diag,
                                "u32_rtol_1e-06": float(np.abs(uc - u64h).max()) / diag},
+        "restarts": restarts,
         "f32_tight_solve": {"result": st_t.result.name, "iters": st_t.n_steps,
                             "rel_grad": st_t.grad_norm / st_t.grad_norm_first},
         "fp64_solve": {"result": sol64.result.name, "iters": sol64.n_steps, "seconds": t64,
@@ -314,7 +335,7 @@ def headline_accuracy(pot, model, m, mu, lam, mask, fv, u0, u32, dev, n_mid=100,
     }
 
 
-def _solve_f64(m, mu, lam, mask, fv, rtol, dev, max_steps=40000):
+def _solve_f64(m, mu, lam, mask, fv, rtol, dev, max_steps=40000, u_init=None):
     import numpy as np
     import torch
 
@@ -330,7 +351,7 @@ def _solve_f64(m, mu, lam, mask, fv, rtol, dev, max_steps=40000):
     b.add_potential(ag.StableNeoHookean.from_pyvista(mesh, dtype=torch.float64))
     model = b.finalize()
     sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=max_steps, rtol=rtol)).solver(ag.ForwardProblem(model))
-    sv.reset(torch.tensor(np.where(mask, fv, 0.0), dtype=torch.float64, device=dev))
+    sv.reset(torch.tensor(np.where(mask, fv, 0.0), dtype=torch.float64, device=dev) if u_init is None else u_init)
     sv.iterate(max_steps)
     u = torch.empty((m.n_points, 3), dtype=torch.float64, device=dev)
     sol = sv.read(u)
@@ -1203,8 +1224,9 @@ def run_irregular_study(a) -> None:
     by Jacobi-preconditioned PNCG in FP32 and FP64 on the GPU and by the FP64
     C restatement of the reference's PNCG on the host, with the workload's
     stiffness contrast (mu log-uniform over three decades) and with a uniform
-    mu (the contrast's geometric mean).  ||g|| / ||g0|| is recorded at fixed
-    iteration counts."""
+    mu (the contrast's geometric mean); FP32 also with the reference-state
+    correction refreshed at every 2x drop of ||g|| (default: 100x) and without
+    it.  ||g|| / ||g0|| is recorded at fixed iteration counts."""
     import numpy as np
     import torch
 
@@ -1233,7 +1255,7 @@ def run_irregular_study(a) -> None:
         mesh.cell_data["lambda"] = 10.0 * mu
         mesh.point_data["FixedMask"] = mask
         mesh.point_data["FixedValue"] = np.zeros((pts.shape[0], 3))
-        for dt in (torch.float32, torch.float64):
+        for dt, refresh in ((torch.float32, -1.0), (torch.float32, 0.5), (torch.float32, 0.0), (torch.float64, -1.0)):
             b = ag.ModelBuilder(dtype=dt)
             b.add_vertices(mesh)
             b.add_fixed(mesh)
@@ -1242,7 +1264,8 @@ def run_irregular_study(a) -> None:
             fm.point_data["Force"] = f
             fm.point_data["GlobalPointId"] = np.arange(pts.shape[0])
             b.add_potential(ag.ExternalForce.from_pyvista(fm, dtype=dt))
-            sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=10**6, rtol=0.0)).solver(ag.ForwardProblem(b.finalize()))
+            sv = ag.PNCG(ag.ConvergenceCriteria(max_steps=10**6, rtol=0.0),
+                         refresh_ratio=refresh).solver(ag.ForwardProblem(b.finalize()))
             sv.reset(torch.zeros((pts.shape[0], 3), dtype=dt, device=dev))
             done, traj = 0, {}
             for k in marks:
@@ -1251,7 +1274,9 @@ def run_irregular_study(a) -> None:
                 st = sv.read()
                 traj[k] = {"rel_grad": st.grad_norm / st.grad_norm_first, "result": st.result.name,
                            "iters": st.n_steps}
-            rec["gpu_" + ("f32" if dt == torch.float32 else "f64")] = traj
+            key = "gpu_f64" if dt == torch.float64 else {-1.0: "gpu_f32", 0.5: "gpu_f32_refresh_0.5",
+                                                          0.0: "gpu_f32_no_correction"}[refresh]
+            rec[key] = traj
         dhdX, dV = O.region_compute_grad(pts, cells)
         cm = build_c.CModel(1, cells, dhdX, dV, mu, 10.0 * mu, pts.shape[0], mask=mask.astype(np.uint8), force=f)
         traj = {}
