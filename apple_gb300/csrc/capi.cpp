@@ -764,7 +764,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   AGB_REQUIRE(prm.max_steps >= 0 && prm.max_backtracking >= 0 && prm.max_backtracking <= 60 &&
                   prm.refresh_ratio < 1.0,
               AGB_E_INVALID, "agb_solver_create: bad parameters");
-  if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-2 : 0.0;
+  if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-1 : 0.0;
   agb_solver* sv = new (std::nothrow) agb_solver();
   AGB_REQUIRE(sv, AGB_E_INVALID, "agb_solver_create: out of host memory");
   sv->model = m;
@@ -1467,7 +1467,7 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
               "agb_batch_create: bad parameters");
   if (chunk_verts <= 0) chunk_verts = 512;
   AGB_REQUIRE(prm.refresh_ratio < 1.0, AGB_E_INVALID, "agb_batch_create: bad parameters");
-  if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-2 : 0.0;
+  if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-1 : 0.0;
   const bool delta = prec == AGB_F32 && prm.refresh_ratio > 0.0;
   agb_batch* b = new (std::nothrow) agb_batch();
   AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_create: out of host memory");

@@ -157,10 +157,13 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
 }
 
 // ---------------------------------------------------------------------------
-// ARAP trial pass: remainders at trial steps alpha_0 2^-j, j = j0 .. j0+2
+// ARAP trial pass: remainders at trial steps alpha_0 2^-j, j = j0 .. j0+nt-1
+// (nt <= 3).  The first launch of an iteration tries alpha_0 alone, which the
+// Armijo test accepts on most iterations; the later ones, which return at
+// once once a step is decided, try three halvings each.
 // ---------------------------------------------------------------------------
 template <class R>
-__global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a, int j0) {
+__global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a, int j0, int nt) {
   __shared__ R sh[3][kTileVerts];
   __shared__ R sl[3][kTileVerts];
   __shared__ R sp[3][kTileVerts];
@@ -189,7 +192,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
     Svd<R> base;
     svd_rv(G, (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G), base);
 #pragma unroll 1
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < nt; ++j) {
       R Gt[3][3];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
     return;
   if (threadIdx.x != 0) return;
   const double gd = st->gd;
-  for (int j = 0; j < 3; ++j) {
+  for (int j = 0; j < nt; ++j) {
     const int J = j0 + j;
     if (J > st->max_bt) break;
     const double t = ldexp(a0, -J);
@@ -224,7 +227,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
       return;
     }
   }
-  if (j0 + 2 >= st->max_bt) {
+  if (j0 + nt - 1 >= st->max_bt) {
     reject_step(st, st->max_bt);
     st->decided = 1;
   }
@@ -509,7 +512,9 @@ static cudaError_t launch_iteration_d(const SolveArgs& a, bool use_cond, bool fi
       solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, use_cond ? 1 : 0);
     }
     if constexpr (MAT == AGB_ARAP) {
-      for (int j0 = 0; j0 <= max_bt; j0 += 3) solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0);
+      solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, 0, 1);
+      for (int j0 = 1; j0 <= max_bt; j0 += 3)
+        solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0, max_bt - j0 + 1 < 3 ? max_bt - j0 + 1 : 3);
     }
   }
   cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a);

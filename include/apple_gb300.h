@@ -199,7 +199,7 @@ typedef struct agb_pncg_params {
   double beta_max;             /* |beta| above this resets to steepest descent (10) */
   double refresh_ratio;        /* FP32 stable Neo-Hookean: reference-state correction, refreshing
                                   the FP64 reference gradient whenever ||g|| has dropped by this
-                                  factor; 0: off; < 0 (default): 1e-2 when rtol < 1e-5 asks for
+                                  factor; 0: off; < 0 (default): 1e-1 when rtol < 1e-5 asks for
                                   more than FP32 element forces resolve, else off */
 } agb_pncg_params;
 
