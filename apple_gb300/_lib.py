@@ -96,6 +96,8 @@ _SIGNATURES = {
         c_int,
         [c_void_p, c_uint, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     ),
+    "agb_dof_to_free": (c_int, [c_int32, ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "agb_dof_to_full": (c_int, [c_int32, ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "agb_pncg_default_params": (None, [POINTER(PncgParams)]),
     "agb_solver_create": (c_int, [c_void_p, POINTER(PncgParams), POINTER(c_void_p)]),
     "agb_solver_destroy": (c_int, [c_void_p]),

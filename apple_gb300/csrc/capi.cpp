@@ -666,6 +666,26 @@ int agb_model_create(agb_space* space, int precision, int32_t n_pot, agb_fem* co
   return AGB_OK;
 }
 
+int agb_dof_to_free(int32_t precision, int64_t n_free, const int64_t* free_index, const void* full,
+                    void* free_out, void* stream) {
+  clear_error();
+  AGB_REQUIRE(precision == AGB_F32 || precision == AGB_F64, AGB_E_INVALID, "agb_dof_to_free: bad precision");
+  AGB_REQUIRE(n_free >= 0, AGB_E_INVALID, "agb_dof_to_free: negative size");
+  AGB_REQUIRE(n_free == 0 || (free_index && full && free_out), AGB_E_INVALID, "agb_dof_to_free: null argument");
+  return check_launch(launch_dof_to_free(precision, n_free, free_index, full, free_out, as_stream(stream)),
+                      "dof_to_free");
+}
+
+int agb_dof_to_full(int32_t precision, int64_t n_full, const int32_t* slot, const void* free_in,
+                    const void* fill, void* full_out, void* stream) {
+  clear_error();
+  AGB_REQUIRE(precision == AGB_F32 || precision == AGB_F64, AGB_E_INVALID, "agb_dof_to_full: bad precision");
+  AGB_REQUIRE(n_full >= 0, AGB_E_INVALID, "agb_dof_to_full: negative size");
+  AGB_REQUIRE(n_full == 0 || (slot && full_out), AGB_E_INVALID, "agb_dof_to_full: null argument");
+  return check_launch(launch_dof_to_full(precision, n_full, slot, free_in, fill, full_out, as_stream(stream)),
+                      "dof_to_full");
+}
+
 int agb_model_eval(agb_model* m, unsigned flags, const void* u, const void* p, double* energy,
                    void* grad, void* diag, void* prod, double* quad, void* stream) {
   AGB_REQUIRE(m && u, AGB_E_INVALID, "agb_model_eval: null handle or u");
@@ -731,12 +751,17 @@ int agb_solver_destroy(agb_solver* sv) {
   for (void* p : {(void*)sv->d_tile_estart, (void*)sv->d_tile_vstart, (void*)sv->d_tile_gstart,
                   (void*)sv->d_group_estart, (void*)sv->d_tv_vid,
                   (void*)sv->d_slot_of_tv, sv->d_rec, (void*)sv->d_ids, sv->d_xa, sv->d_gd, sv->d_p0,
-                  sv->d_p1, sv->d_xref, sv->d_gref, sv->d_slots, sv->d_part, (void*)sv->d_cnt, (void*)sv->d_state,
-                  sv->d_u_tmp, sv->d_act})
+                  sv->d_p1, sv->d_xref, sv->d_gref, sv->d_svd, sv->d_slots, sv->d_part, (void*)sv->d_cnt,
+                  (void*)sv->d_state, sv->d_u_tmp, sv->d_act})
     dfree(p);
   if (sv->h_state) cudaFreeHost(sv->h_state);
   delete sv;
   return AGB_OK;
+}
+
+// ARAP: both per-element SVD caches, 3 V4 per cell each
+static size_t svd_cache_bytes(const agb_solver* sv) {
+  return 2 * 3 * v4_bytes(sv->precision) * (size_t)sv->fv.n_cells;
 }
 
 int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** out) {
@@ -854,6 +879,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   const bool delta = sv->precision == AGB_F32 && mat != AGB_ARAP && prm.refresh_ratio > 0.0;
   if (!rc && delta) rc = dalloc_bytes(&sv->d_xref, v4 * np);
   if (!rc && delta) rc = dalloc_bytes(&sv->d_gref, v4 * np);
+  if (!rc && mat == AGB_ARAP) rc = dalloc_bytes(&sv->d_svd, svd_cache_bytes(sv));
   if (!rc) rc = dalloc_bytes(&sv->d_slots, v4 * 2 * (size_t)m->n_slots);
   if (!rc) rc = dalloc_bytes(&sv->d_part, 8 * n_part);
   if (!rc) rc = dalloc(&sv->d_cnt, n_cnt);
@@ -894,6 +920,7 @@ int agb_solver_create(agb_model* m, const agb_pncg_params* params, agb_solver** 
   a.p1 = sv->d_p1;
   a.xref = sv->d_xref;
   a.gref = sv->d_gref;
+  a.svd = sv->d_svd;
   a.delta = delta ? 1 : 0;
   a.force = m->d_force;
   a.slot_of_tv = sv->d_slot_of_tv;
@@ -1161,18 +1188,19 @@ int agb_solver_read_reductions(agb_solver* sv, double* out5, void* stream) {
 }
 
 // checkpoint layout: header, then xa (2 V4 per vertex), gd (2 V4), p0, p1,
-// [xref, gref when the FP32 correction is on], SolverState
+// [xref, gref when the FP32 correction is on], [the two SVD caches (ARAP)],
+// SolverState
 struct CheckpointHeader {
   uint64_t magic;
   int32_t version, precision, n_points, delta, state_bytes, pad;
   uint64_t fingerprint;  // solver_fingerprint of the saving solver
 };
 constexpr uint64_t kCheckpointMagic = 0x4147424350544b31ull;  // "AGBCPTK1"
-constexpr int32_t kCheckpointVersion = 2;
+constexpr int32_t kCheckpointVersion = 3;
 
 static size_t checkpoint_vec_bytes(const agb_solver* sv) {
   const size_t v4 = v4_bytes(sv->precision) * (size_t)sv->args.n_points;
-  return 2 * v4 + 2 * v4 + v4 + v4 + (sv->args.delta ? 2 * v4 : 0);
+  return 2 * v4 + 2 * v4 + v4 + v4 + (sv->args.delta ? 2 * v4 : 0) + (sv->d_svd ? svd_cache_bytes(sv) : 0);
 }
 
 int agb_solver_checkpoint_size(agb_solver* sv, size_t* bytes) {
@@ -1188,6 +1216,7 @@ static std::vector<std::pair<void*, size_t>> checkpoint_arrays(agb_solver* sv) {
     a.push_back({sv->d_xref, v4});
     a.push_back({sv->d_gref, v4});
   }
+  if (sv->d_svd) a.push_back({sv->d_svd, svd_cache_bytes(sv)});
   a.push_back({(void*)sv->d_state, sizeof(SolverState)});
   return a;
 }

@@ -621,4 +621,70 @@ __device__ __forceinline__ R arap_remainder(const Svd<R>& base, const Svd<R>& tr
   return R(0.5) * mu * (a + b);
 }
 
+// ---------------------------------------------------------------------------
+// Proper rotations as unit quaternions q = (w, x, y, z), for the compact
+// per-element SVD that the ARAP solver keeps between passes.
+// Rotation -> quaternion by Shepperd's method (J. Guidance and Control 1(3),
+// 1978): 4w^2 = 1 + tr M, 4x^2 = 1 + M00 - M11 - M22, 4y^2 = 1 - M00 + M11 -
+// M22, 4z^2 = 1 - M00 - M11 + M22 sum to 4, so the largest is at least 1;
+// its component comes from one reciprocal square root and the other three
+// from the sums and differences of the off-diagonal pairs
+// (M21 - M12 = 4wx, M02 - M20 = 4wy, M10 - M01 = 4wz, M01 + M10 = 4xy,
+// M02 + M20 = 4xz, M12 + M21 = 4yz).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ void quat_of_rotation(const R (&M)[3][3], R (&q)[4]) {
+  const R tw = R(1) + M[0][0] + M[1][1] + M[2][2];
+  const R tx = R(1) + M[0][0] - M[1][1] - M[2][2];
+  const R ty = R(1) - M[0][0] + M[1][1] - M[2][2];
+  const R tz = R(1) - M[0][0] - M[1][1] + M[2][2];
+  if (tw >= tx && tw >= ty && tw >= tz) {
+    const R r = rsqrt_(tw), h = R(0.5) * r;
+    q[0] = R(0.5) * tw * r;
+    q[1] = (M[2][1] - M[1][2]) * h;
+    q[2] = (M[0][2] - M[2][0]) * h;
+    q[3] = (M[1][0] - M[0][1]) * h;
+  } else if (tx >= ty && tx >= tz) {
+    const R r = rsqrt_(tx), h = R(0.5) * r;
+    q[0] = (M[2][1] - M[1][2]) * h;
+    q[1] = R(0.5) * tx * r;
+    q[2] = (M[0][1] + M[1][0]) * h;
+    q[3] = (M[0][2] + M[2][0]) * h;
+  } else if (ty >= tz) {
+    const R r = rsqrt_(ty), h = R(0.5) * r;
+    q[0] = (M[0][2] - M[2][0]) * h;
+    q[1] = (M[0][1] + M[1][0]) * h;
+    q[2] = R(0.5) * ty * r;
+    q[3] = (M[1][2] + M[2][1]) * h;
+  } else {
+    const R r = rsqrt_(tz), h = R(0.5) * r;
+    q[0] = (M[1][0] - M[0][1]) * h;
+    q[1] = (M[0][2] + M[2][0]) * h;
+    q[2] = (M[1][2] + M[2][1]) * h;
+    q[3] = R(0.5) * tz * r;
+  }
+}
+
+// the rotation of q / |q| (a stored quaternion is unit only to rounding):
+// M = I + s [[-(y2+z2), xy-wz, xz+wy], [xy+wz, -(x2+z2), yz-wx],
+//            [xz-wy, yz+wx, -(x2+y2)]],  s = 2 / |q|^2
+template <class R>
+__device__ __forceinline__ void rotation_of_quat(const R (&q)[4], R (&M)[3][3]) {
+  const R w = q[0], x = q[1], y = q[2], z = q[3];
+  const R r = rsqrt_(w * w + x * x + y * y + z * z);
+  const R s = R(2) * r * r;
+  const R xx = s * x * x, yy = s * y * y, zz = s * z * z;
+  const R xy = s * x * y, xz = s * x * z, yz = s * y * z;
+  const R wx = s * w * x, wy = s * w * y, wz = s * w * z;
+  M[0][0] = R(1) - (yy + zz);
+  M[0][1] = xy - wz;
+  M[0][2] = xz + wy;
+  M[1][0] = xy + wz;
+  M[1][1] = R(1) - (xx + zz);
+  M[1][2] = yz - wx;
+  M[2][0] = xz - wy;
+  M[2][1] = yz + wx;
+  M[2][2] = R(1) - (xx + yy);
+}
+
 }  // namespace agb

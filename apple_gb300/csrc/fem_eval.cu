@@ -285,4 +285,53 @@ cudaError_t launch_unpack(int precision, int n, const int32_t* uoi, const int32_
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// free/fixed DOF maps (forward/dof_map/_dof_map.py:30-50): one gather each,
+// with coalesced writes; to_full reads a full-length slot map (free index or
+// -1) instead of scattering the free and the fixed values separately
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void dof_to_free_kernel(int64_t n, const int64_t* __restrict__ idx, const R* __restrict__ full,
+                                   R* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = full[idx[i]];
+}
+
+template <class R>
+__global__ void dof_to_full_kernel(int64_t n, const int32_t* __restrict__ slot, const R* __restrict__ free_in,
+                                   const R* __restrict__ fill, R* __restrict__ out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k = slot[j];
+    out[j] = k >= 0 ? free_in[k] : (fill ? fill[j] : R(0));
+  }
+}
+
+static int dof_blocks(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  const int64_t cap = 152 * 8;  // 8 resident 256-thread CTAs on each of the 152 SMs
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+cudaError_t launch_dof_to_free(int precision, int64_t n, const int64_t* idx, const void* full, void* out,
+                               cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (precision == AGB_F64)
+    dof_to_free_kernel<double><<<dof_blocks(n), 256, 0, s>>>(n, idx, (const double*)full, (double*)out);
+  else
+    dof_to_free_kernel<float><<<dof_blocks(n), 256, 0, s>>>(n, idx, (const float*)full, (float*)out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dof_to_full(int precision, int64_t n, const int32_t* slot, const void* free_in,
+                               const void* fill, void* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (precision == AGB_F64)
+    dof_to_full_kernel<double><<<dof_blocks(n), 256, 0, s>>>(n, slot, (const double*)free_in,
+                                                            (const double*)fill, (double*)out);
+  else
+    dof_to_full_kernel<float><<<dof_blocks(n), 256, 0, s>>>(n, slot, (const float*)free_in,
+                                                           (const float*)fill, (float*)out);
+  return cudaGetLastError();
+}
+
 }  // namespace agb

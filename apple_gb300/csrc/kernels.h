@@ -36,4 +36,11 @@ cudaError_t launch_unpack(int precision, int n_points, const int32_t* user_of_in
 
 int unpack_blocks(int n_points);
 
+// free/fixed DOF maps: free[i] = full[free_idx[i]];
+// full[j] = slot[j] >= 0 ? free[slot[j]] : (fill ? fill[j] : 0)
+cudaError_t launch_dof_to_free(int precision, int64_t n_free, const int64_t* free_idx, const void* full,
+                               void* free_out, cudaStream_t stream);
+cudaError_t launch_dof_to_full(int precision, int64_t n_full, const int32_t* slot, const void* free_in,
+                               const void* fill, void* full_out, cudaStream_t stream);
+
 }  // namespace agb

@@ -12,11 +12,17 @@
 //                   dE(t) = t g.p + sum_m C_m t^m -- the same trial points
 //                   and decisions as evaluating fun(x + t p) per trial,
 //                   without the O(1) cancellation of f(x+tp) - f(x)
-//   [ARAP]          trial passes evaluate the remainder at up to three trial
-//                   steps each (ARAP is not polynomial in t)
 //   gradient pass   at x_{k+1} = x_k + t p_k: energy, gradient, clamped
 //                   Hessian diagonal -> tile slots, accumulated per warp in
 //                   private shared-memory copies (no atomics, fixed order)
+//   [ARAP]          (not polynomial in t) the gradient pass evaluates the
+//                   first trial step alpha_0 speculatively, sums the
+//                   elements' energy remainders there and takes the Armijo
+//                   decision; only when it rejects do trial passes (three
+//                   halvings each) and a second gradient pass run.  Each
+//                   element's SVD at x is kept between passes (U and V as
+//                   quaternions, sigma - 1), so the direction pass needs none
+//                   and the trial SVDs start from it.
 //   vertex pass     x_{k+1}, g_{k+1}, d_{k+1}, p_k written; dot products of
 //                   the Dai-Kou beta, the descent check and the convergence
 //                   norm reduced; the last block decides beta_{k+1}, the
@@ -82,6 +88,7 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   const int pb = st->pbuf;
   const V4<R>* pprev = p_prev<R>(a, pb);
   V4<R>* pcur = p_cur<R>(a, pb);
+  const V4<R>* csvd = MAT == AGB_ARAP ? svd_cache<R>(a, st->sbuf) : nullptr;
 
   // pHp and c3..c6 in plain R, c2 (terms of both signs) in float-float
   R plain[N] = {};
@@ -123,9 +130,9 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
 #pragma unroll
         for (int m = 1; m < 5; ++m) plain[1 + m] += c[m];
       } else {
-        const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
+        // the SVD at x, kept by the gradient pass that evaluated x
         Svd<R> sv;
-        svd_rv(G, jm1, sv);
+        svd_get(csvd, (size_t)a.fv.n_cells, e, sv);
         R lk[3];
         arap_lambdas(sv, lk);
         plain[0] += fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0));
@@ -158,9 +165,10 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
 
 // ---------------------------------------------------------------------------
 // ARAP trial pass: remainders at trial steps alpha_0 2^-j, j = j0 .. j0+nt-1
-// (nt <= 3).  The first launch of an iteration tries alpha_0 alone, which the
-// Armijo test accepts on most iterations; the later ones, which return at
-// once once a step is decided, try three halvings each.
+// (nt <= 3), each trial SVD warm-started from the cached one at x.  The
+// speculative gradient pass tests alpha_0 itself; these passes run only when
+// it was rejected (they return at once once a step is decided) and try three
+// halvings each.
 // ---------------------------------------------------------------------------
 template <class R>
 __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a, int j0, int nt) {
@@ -178,6 +186,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
   const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
   const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
   stage_direction<R>(a, vs, nv, p_cur<R>(a, st->pbuf), sh, sl, sp);
+  const V4<R>* cbase = svd_cache<R>(a, st->sbuf);
   __syncthreads();
   Acc<R> sums[3] = {};
   for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a,
     gather_corners(sp, l, w);
     corner_gradient(w, geo.D, dF);
     Svd<R> base;
-    svd_rv(G, (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G), base);
+    svd_get(cbase, (size_t)a.fv.n_cells, e, base);
 #pragma unroll 1
     for (int j = 0; j < nt; ++j) {
       R Gt[3][3];
@@ -246,15 +255,34 @@ size_t solver_grad_smem(int precision) {
 }
 
 template <class R, int MAT, bool DELTA>
-__global__ void __launch_bounds__(kGradThreads, 5) solver_grad_kernel(SolveArgs a) {
-  grad_tile<R, MAT, DELTA>(a, blockIdx.x, a.st);
+__global__ void __launch_bounds__(kGradThreads, 5) solver_grad_kernel(SolveArgs a, int fallback) {
+  grad_tile<R, MAT, DELTA>(a, blockIdx.x, a.st, nullptr, fallback != 0);
+}
+
+// ARAP: the gradient pass at the first trial step x + alpha_0 p, with the
+// Armijo test of that step (grad_tile's SPEC form; the remainders reduce
+// through the trial partials)
+template <class R>
+__global__ void __launch_bounds__(kGradThreads, 4) solver_grad_spec_kernel(SolveArgs a) {
+  __shared__ Acc<R> red[kGradWarps];
+  Acc<R> rem[1] = {};
+  if (!grad_tile<R, AGB_ARAP, false, true>(a, blockIdx.x, a.st, &rem[0])) return;
+  double tot[1];
+  if (!grid_reduce2<1, 0x1u, R>(rem, (AccStore<R>*)a.part_t, (AccStore<R>*)a.gpart_t, a.cnt_t, gridDim.x, red,
+                                tot))
+    return;
+  if (threadIdx.x == 0) spec_decide(a.st, tot[0]);
 }
 
 // ---------------------------------------------------------------------------
 // vertex pass
 // ---------------------------------------------------------------------------
+// phase (ARAP): 1 after the speculative gradient pass, running only if its
+// step was accepted; 2 after the fallback passes, running only if it was not;
+// 0 otherwise (always runs)
 template <class R, bool DELTA>
-__global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_kernel(SolveArgs a, int use_cond) {
+__global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_kernel(SolveArgs a, int use_cond,
+                                                                                   int phase) {
   constexpr int N = 12;
   __shared__ Acc<R> red[(kVThreads / 32) * N];
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,6 +300,9 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
     return;
   }
   if (guard_skip(a, st)) return;  // the loop condition stays as the direction pass left it: 0
+  // ARAP: the pass after the speculative gradient pass, or the one after the
+  // fallback passes, whichever applies (the other leaves the condition alone)
+  if ((phase == 1 && !st->spec_ok) || (phase == 2 && st->spec_ok)) return;
   const R t = (R)st->t;
   const V4<R>* P = p_cur<R>(a, st->pbuf);
   // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
@@ -296,6 +327,7 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
   if (!grid_reduce_masked<N, FF, R>(acc, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
   if (threadIdx.x != 0) return;
   vertex_decide(st, tot);
+  if (a.svd) st->sbuf ^= 1;  // the gradient pass's SVDs are those at the new x
   const bool go = !st->done && st->iter < st->iter_limit;
   if (use_cond)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
@@ -402,6 +434,8 @@ __global__ void solver_init_kernel(SolveArgs a, const R* __restrict__ u, const V
     st->pbuf = 0;
     st->refresh = 0;
     st->gnorm_ref = 0.0;
+    st->sbuf = 0;
+    st->spec_ok = 0;
   }
 }
 
@@ -426,6 +460,7 @@ static cudaError_t prepare_t() {
   const int g = (int)grad_smem_bytes<R>();
   const cudaFuncAttribute m = cudaFuncAttributeMaxDynamicSharedMemorySize;
   cudaError_t e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_ARAP, false>, m, g);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_spec_kernel<R>, m, (int)grad_spec_smem_bytes<R>());
   if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN, false>, m, g);
   if (e == cudaSuccess && kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>)
     e = cudaFuncSetAttribute(solver_grad_kernel<R, AGB_STABLE_NEO_HOOKEAN, kRefDelta<R, AGB_STABLE_NEO_HOOKEAN>>, m, g);
@@ -512,14 +547,25 @@ static cudaError_t launch_iteration_d(const SolveArgs& a, bool use_cond, bool fi
       solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, use_cond ? 1 : 0);
     }
     if constexpr (MAT == AGB_ARAP) {
-      solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, 0, 1);
+      // speculative gradient pass at alpha_0 and its vertex pass; when the
+      // step is rejected, trial passes from alpha_0 / 2, then the gradient
+      // and vertex passes at the step they decide (each of these returns at
+      // once when the speculative step was accepted)
+      const dim3 gb(kGradThreads), vg(a.vblocks), vb(kVThreads);
+      const int uc = use_cond ? 1 : 0;
+      cudaError_t e = launch_pdl(solver_grad_spec_kernel<R>, eg, gb, grad_spec_smem_bytes<R>(), s, a);
+      if (e == cudaSuccess) e = launch_pdl(solver_vertex_kernel<R, DELTA>, vg, vb, 0, s, a, uc, 1);
+      if (e != cudaSuccess) return e;
       for (int j0 = 1; j0 <= max_bt; j0 += 3)
         solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0, max_bt - j0 + 1 < 3 ? max_bt - j0 + 1 : 3);
+      e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, gb, grad_smem_bytes<R>(), s, a, 1);
+      if (e != cudaSuccess) return e;
+      return launch_pdl(solver_vertex_kernel<R, DELTA>, vg, vb, 0, s, a, uc, 2);
     }
   }
-  cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a);
+  cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a, 0);
   if (e != cudaSuccess) return e;
-  return launch_pdl(solver_vertex_kernel<R, DELTA>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond ? 1 : 0);
+  return launch_pdl(solver_vertex_kernel<R, DELTA>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond ? 1 : 0, 0);
 }
 
 template <class R, int MAT>
@@ -560,8 +606,13 @@ template <class R, int MAT, bool DELTA>
 static cudaError_t launch_pass_d(const SolveArgs& a, int which, cudaStream_t s) {
   const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
   if (which == 0) solver_dir_kernel<R, MAT><<<dir_blocks(a.fv.n_tiles), eb, 0, s>>>(a, 0);
-  if (which == 1) solver_grad_kernel<R, MAT, DELTA><<<eg, kGradThreads, grad_smem_bytes<R>(), s>>>(a);
-  if (which == 2) solver_vertex_kernel<R, DELTA><<<a.vblocks, kVThreads, 0, s>>>(a, 0);
+  if (which == 1) {
+    if constexpr (MAT == AGB_ARAP)  // the iteration's gradient pass is the speculative one
+      solver_grad_spec_kernel<R><<<eg, kGradThreads, grad_spec_smem_bytes<R>(), s>>>(a);
+    else
+      solver_grad_kernel<R, MAT, DELTA><<<eg, kGradThreads, grad_smem_bytes<R>(), s>>>(a, 0);
+  }
+  if (which == 2) solver_vertex_kernel<R, DELTA><<<a.vblocks, kVThreads, 0, s>>>(a, 0, 0);
   return cudaGetLastError();
 }
 

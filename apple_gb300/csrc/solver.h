@@ -46,6 +46,12 @@ struct SolverState {
   int32_t refresh;     // the refresh passes run after this iteration's vertex pass
   double gnorm_ref;    // ||g|| at the last refresh
   double ref_ratio;    // 0: off
+  // ARAP: svd[sbuf] holds each element's SVD at x; the gradient passes write
+  // svd[sbuf ^ 1] and the vertex pass that moves x flips sbuf.  spec_ok: the
+  // speculative gradient pass at alpha_0 passed the Armijo test, so its
+  // gradient is the iteration's and the fallback passes return at once.
+  int32_t sbuf;
+  int32_t spec_ok;
 };
 
 // Everything a solver kernel needs, by value.
@@ -98,6 +104,9 @@ struct SolveArgs {
   // (with no effect) when the first one ended the solve, reached the
   // iteration limit or asked for a refresh
   int guard;
+  // ARAP: two per-element SVD caches, each V4<R>[3][n_cells] (U and V as
+  // quaternions (w x y z), then (sigma - 1, 0)); null for other materials
+  void* svd;
 };
 
 cudaError_t launch_solver_init(const SolveArgs& a, const void* u_user, const void* fixed,
@@ -235,6 +244,7 @@ struct agb_solver {
   void* d_p1 = nullptr;
   void* d_xref = nullptr;  // reference state (FP32 stable Neo-Hookean)
   void* d_gref = nullptr;
+  void* d_svd = nullptr;   // ARAP: two per-element SVD caches (SolveArgs::svd)
   void* d_slots = nullptr;
   void* d_part = nullptr;
   unsigned* d_cnt = nullptr;

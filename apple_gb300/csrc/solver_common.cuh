@@ -56,6 +56,33 @@ __device__ __forceinline__ V4<R>* p_cur(const SolveArgs& a, int pb) {
   return (V4<R>*)(pb ? a.p0 : a.p1);
 }
 
+// ARAP: the per-element SVD cache svd[b] (SolveArgs::svd)
+template <class R>
+__device__ __forceinline__ V4<R>* svd_cache(const SolveArgs& a, int b) {
+  return (V4<R>*)a.svd + (size_t)b * 3 * (size_t)a.fv.n_cells;
+}
+template <class R>
+__device__ __forceinline__ void svd_put(V4<R>* c, size_t n, int e, const Svd<R>& d) {
+  R q[4];
+  quat_of_rotation(d.U, q);
+  c[e] = V4<R>{q[0], q[1], q[2], q[3]};
+  quat_of_rotation(d.V, q);
+  c[n + e] = V4<R>{q[0], q[1], q[2], q[3]};
+  c[2 * n + e] = V4<R>{d.sm1[0], d.sm1[1], d.sm1[2], R(0)};
+}
+template <class R>
+__device__ __forceinline__ void svd_get(const V4<R>* c, size_t n, int e, Svd<R>& d) {
+  const V4<R> u = ldg4(c + e), v = ldg4(c + n + e), m = ldg4(c + 2 * n + e);
+  const R qu[4] = {u.x, u.y, u.z, u.w}, qv[4] = {v.x, v.y, v.z, v.w};
+  rotation_of_quat(qu, d.U);
+  rotation_of_quat(qv, d.V);
+  d.sm1[0] = m.x;
+  d.sm1[1] = m.y;
+  d.sm1[2] = m.z;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d.s[k] = R(1) + d.sm1[k];
+}
+
 template <class R>
 __device__ __forceinline__ void stage_direction(const SolveArgs& a, int vs, int nv, const V4<R>* P,
                                                 R (*sh)[kTileVerts], R (*sl)[kTileVerts],
@@ -149,6 +176,11 @@ __host__ __device__ constexpr size_t grad_smem_bytes() {
   // staged hi (V4: x y z lo.x) and lo (V2: lo.y lo.z) + per-warp accumulators (V4 + V2)
   return (size_t)kTileVerts * (size_t)(kGradWarps + 1) * (sizeof(V4<R>) + sizeof(V2<R>));
 }
+// the speculative ARAP gradient pass also stages p
+template <class R>
+__host__ __device__ constexpr size_t grad_spec_smem_bytes() {
+  return grad_smem_bytes<R>() + (size_t)kTileVerts * sizeof(V4<R>);
+}
 
 
 // x + t p as hi + lo pairs: (hi.x hi.y hi.z lo.x) and (lo.y lo.z) per vertex
@@ -169,6 +201,23 @@ __device__ __forceinline__ void stage_point(const SolveArgs& a, const int (&vid)
     pair_add(hz, lz, mul_rn(t, p.z));
     sh[i] = V4<R>{hx, hy, hz, lx};
     sl[i] = V2<R>{ly, lz};
+  }
+}
+
+// x as hi + lo pairs (as stage_point with t = 0) and p, for the speculative
+// ARAP gradient pass
+template <class R>
+__device__ __forceinline__ void stage_point_dir(const SolveArgs& a, const int (&vid)[kGradVerts], const V4<R>* P,
+                                                V4<R>* sh, V2<R>* sl, V4<R>* sp) {
+  const V4<R>* XA = (const V4<R>*)a.xa;
+#pragma unroll
+  for (int j = 0; j < kGradVerts; ++j) {
+    const int v = vid[j], i = threadIdx.x + j * kGradThreads;
+    if (v < 0) continue;
+    const V4<R> x = ldg4(XA + 2 * v), xl = ldg4(XA + 2 * v + 1), p = ldg4(P + v);
+    sh[i] = V4<R>{x.x, x.y, x.z, xl.x};
+    sl[i] = V2<R>{xl.y, xl.z};
+    sp[i] = V4<R>{p.x, p.y, p.z, R(0)};
   }
 }
 
@@ -225,8 +274,32 @@ __device__ __forceinline__ void dir_decide(SolverState* st, const double* tot) {
     }
     st->decided = 1;
   } else {
+    // ARAP: the speculative gradient pass evaluates alpha_0
     st->t = 0.0;
     st->decided = 0;
+    st->spec_ok = 0;
+  }
+}
+
+// Last block of the speculative ARAP gradient pass (thread 0): the Armijo
+// test of the first trial step t = alpha_0 on dE = t g.p + sum of the
+// elements' remainders.  Accepted: the pass's gradient is the iteration's.
+// Rejected: the trial passes go on from alpha_0 / 2, as the reference's
+// backtracking does, and a fallback gradient pass evaluates the step they
+// decide.
+__device__ __forceinline__ void spec_decide(SolverState* st, double rem) {
+  const double t = st->alpha0, gd = st->gd;
+  const double de = gd * t + rem;
+  if (isfinite(de) && de <= st->armijo_c * t * gd) {
+    st->t = t;
+    st->delta_e = de;
+    st->ls_ok = 1;
+    st->ls_steps = 0;
+    st->decided = 1;
+    st->spec_ok = 1;
+  } else if (st->max_bt <= 0) {
+    reject_step(st, 0);
+    st->decided = 1;
   }
 }
 
@@ -444,28 +517,39 @@ __device__ __forceinline__ void delta_gradient(const V4<R>* sh, const V2<R>* sl,
 }
 
 // The gradient pass over one tile (one CTA of kGradThreads threads, dynamic
-// shared memory grad_smem_bytes<R>()): stage x + t p, per warp group forces
-// and clamped diagonal into the warp's private accumulator, then one slot per
-// tile vertex.  (The energy is not needed by the iteration; energy_tile
-// evaluates it on demand.)  st is the state of
-// the tile's mesh; the first group's record, the vertex ids and the slot
-// indices are read before the dependency wait.
-template <class R, int MAT, bool DELTA = kRefDelta<R, MAT>>
-__device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const SolverState* st) {
+// shared memory grad_smem_bytes<R>(), plus kTileVerts V4<R> with SPEC): stage
+// x + t p, per warp group forces and clamped diagonal into the warp's private
+// accumulator, then one slot per tile vertex.  (The energy is not needed by
+// the iteration; energy_tile evaluates it on demand.)  st is the state of the
+// tile's mesh; the first group's record, the vertex ids and the slot indices
+// are read before the dependency wait.
+//
+// ARAP keeps each element's SVD at x in svd[sbuf] and writes the SVD at the
+// evaluated point into svd[sbuf ^ 1].  SPEC (ARAP, speculative): the pass
+// evaluates at x + alpha_0 p, with the SVD warm-started from the cached one
+// at x, and adds each element's line-search remainder
+// Psi(F + t dF) - Psi(F) - t P(F):dF into *rem, so that the Armijo test of
+// the first trial step needs no pass of its own.  FALLBACK: a pass launched
+// after the speculative one that returns at once unless that one's step was
+// rejected.  Returns false when the pass returned without work.
+template <class R, int MAT, bool DELTA = kRefDelta<R, MAT>, bool SPEC = false>
+__device__ __forceinline__ bool grad_tile(const SolveArgs& a, int tile, const SolverState* st,
+                                          Acc<R>* rem = nullptr, bool fallback = false) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V4<R>* sh = reinterpret_cast<V4<R>*>(smem_raw);
   V4<R>* acc4 = sh + kTileVerts;  // [warp][vertex]: gx gy gz dx
   V2<R>* sl = reinterpret_cast<V2<R>*>(acc4 + kGradWarps * kTileVerts);
   V2<R>* acc2 = sl + kTileVerts;  // [warp][vertex]: dy dz
+  V4<R>* sp = reinterpret_cast<V4<R>*>(acc2 + kGradWarps * kTileVerts);  // SPEC: p
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gs = a.fv.tile_gstart[tile], ge = a.fv.tile_gstart[tile + 1];
   // constant inputs: the first group's element record
   int g = gs + warp;
-  int n = 0;
+  int n = 0, e0 = 0;
   ElemGeo<R> geo;
   uint32_t ids = 0;
   if (g < ge) {
-    const int e0 = a.fv.group_estart[g];
+    e0 = a.fv.group_estart[g];
     n = a.fv.group_estart[g + 1] - e0;
     if (lane < n) load_elem_m<R, MAT>(a.fv, e0 + lane, geo, ids);
   }
@@ -479,11 +563,29 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
   }
   pdl_trigger();
   pdl_wait();
-  if (st->done || guard_skip(a, st)) return;
-  if constexpr (DELTA)
-    stage_point_delta<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
-  else
-    stage_point<R>(a, vid, p_cur<R>(a, st->pbuf), (R)st->t, sh, sl);
+  if (st->done || guard_skip(a, st)) return false;
+  if (fallback && st->spec_ok) return false;
+  // ARAP: base SVDs (x) and the SVDs written by this pass
+  const size_t ncell = (size_t)a.fv.n_cells;
+  const V4<R>* cbase = nullptr;
+  V4<R>* cnext = nullptr;
+  if constexpr (MAT == AGB_ARAP) {
+    if (a.svd) {
+      cbase = svd_cache<R>(a, st->sbuf);
+      cnext = svd_cache<R>(a, st->sbuf ^ 1);
+    }
+  }
+  R t;
+  if constexpr (SPEC) {
+    t = (R)st->alpha0;
+    stage_point_dir<R>(a, vid, p_cur<R>(a, st->pbuf), sh, sl, sp);
+  } else {
+    t = (R)st->t;
+    if constexpr (DELTA)
+      stage_point_delta<R>(a, vid, p_cur<R>(a, st->pbuf), t, sh, sl);
+    else
+      stage_point<R>(a, vid, p_cur<R>(a, st->pbuf), t, sh, sl);
+  }
   for (int i = threadIdx.x; i < kGradWarps * kTileVerts; i += blockDim.x) {
     acc4[i] = V4<R>{R(0), R(0), R(0), R(0)};
     acc2[i] = V2<R>{R(0), R(0)};
@@ -495,11 +597,11 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
   while (g < ge) {
     // prefetch the warp's next group while this one computes
     const int gn = g + kGradWarps;
-    int nn = 0;
+    int nn = 0, e0n = 0;
     ElemGeo<R> geon;
     uint32_t idsn = 0;
     if (gn < ge) {
-      const int e0n = a.fv.group_estart[gn];
+      e0n = a.fv.group_estart[gn];
       nn = a.fv.group_estart[gn + 1] - e0n;
       if (lane < nn) load_elem_m<R, MAT>(a.fv, e0n + lane, geon, idsn);
     }
@@ -507,7 +609,29 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
     R f[4][3], hd[4][3];
     if (lane < n) {
       R G[3][3], P[3][3];
-      if constexpr (DELTA) {
+      if constexpr (SPEC) {
+        // trial point x + t p: G + t dF, its SVD warm-started from the one at x
+        R dF[3][3];
+        pair_gradient(sh, sl, l, geo.D, G);
+        vec_gradient(sp, l, geo.D, dF);
+        Svd<R> base, sv;
+        svd_get(cbase, ncell, e0 + lane, base);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            G[i][k] = fma_rn(t, dF[i][k], G[i][k]);
+            sv.V[i][k] = base.V[i][k];
+          }
+        svd_rv<R, true>(G, (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G), sv);
+        rem->add(arap_remainder(base, sv, t, dF, geo.mu));
+        svd_put(cnext, ncell, e0 + lane, sv);
+        arap_pk1(sv, geo.mu, P);
+        corner_vjp(P, geo.D, f);
+        R lk[3];
+        arap_lambdas(sv, lk);
+        arap_hess_diag(sv, lk, geo.D, geo.mu, hd);
+      } else if constexpr (DELTA) {
         // f_e(x) - f_e(x_ref) from P(A + dG) - P(A); energy and diagonal at A + dG
         R dG[3][3];
         delta_gradient(sh, sl, l, geo.D, G, dG);
@@ -530,6 +654,7 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
         const R jm1 = (G[0][0] + G[1][1] + G[2][2]) + inv2(G) + det3(G);
         Svd<R> sv;
         svd_rv(G, jm1, sv);
+        if (cnext) svd_put(cnext, ncell, e0 + lane, sv);
         arap_pk1(sv, geo.mu, P);
         corner_vjp(P, geo.D, f);
         R lk[3];
@@ -557,6 +682,7 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
     __syncwarp();
     g = gn;
     n = nn;
+    e0 = e0n;
     geo = geon;
     ids = idsn;
   }
@@ -582,6 +708,7 @@ __device__ __forceinline__ void grad_tile(const SolveArgs& a, int tile, const So
     slots[2 * sidx[j]] = V4<R>{q4.x, q4.y, q4.z, R(0)};
     slots[2 * sidx[j] + 1] = V4<R>{q4.w, q2.x, q2.y, R(0)};
   }
+  return true;
 }
 
 // ---------------------------------------------------------------------------

@@ -23,7 +23,11 @@ from .region import FIXED_MASK, FIXED_VALUE, GLOBAL_POINT_ID, mesh_points, point
 
 
 class DofMap:
-    """Free/fixed DOF gather and scatter over the flattened (n_points*3) vector."""
+    """Free/fixed DOF gather and scatter over the flattened (n_points*3) vector
+    (forward/dof_map/_dof_map.py:10-50).  Each map is one kernel of the C
+    library (``agb_dof_to_free`` / ``agb_dof_to_full``) on the caller's
+    current stream; ``to_full`` gathers through a full-length slot map (the
+    DOF's free index, or -1 for a fixed DOF) with the fixed values as fill."""
 
     def __init__(self, n_points: int, fixed_mask: np.ndarray, fixed_values: np.ndarray, *, dim: int = 3,
                  device=None, dtype=torch.float32):
@@ -33,10 +37,18 @@ class DofMap:
         self.fixed_values_full = np.asarray(fixed_values, np.float64).reshape(n_points, dim)
         device = device or torch.device("cuda", torch.cuda.current_device())
         flat = self.fixed_mask.reshape(-1)
-        self.fixed_indices = torch.as_tensor(np.flatnonzero(flat), device=device)
-        self.free_indices = torch.as_tensor(np.flatnonzero(~flat), device=device)
-        self.fixed_values = torch.as_tensor(self.fixed_values_full.reshape(-1)[np.flatnonzero(flat)],
-                                            dtype=dtype, device=device)
+        fixed = np.flatnonzero(flat)
+        free = np.flatnonzero(~flat)
+        self.fixed_indices = torch.as_tensor(fixed, device=device)
+        self.free_indices = torch.as_tensor(free, device=device)
+        self.fixed_values = torch.as_tensor(self.fixed_values_full.reshape(-1)[fixed], dtype=dtype, device=device)
+        slot = np.full(flat.size, -1, np.int32)
+        slot[free] = np.arange(free.size, dtype=np.int32)
+        self.slot = torch.as_tensor(slot, device=device)
+        fill = np.zeros(flat.size)
+        fill[fixed] = self.fixed_values_full.reshape(-1)[fixed]
+        self._fill64 = fill
+        self._fill: dict[torch.dtype, torch.Tensor] = {}
         self.dtype = dtype
 
     @property
@@ -51,22 +63,53 @@ class DofMap:
     def n_full(self) -> int:
         return self.n_points * self.dim
 
+    def _fill_for(self, dtype: torch.dtype) -> torch.Tensor:
+        f = self._fill.get(dtype)
+        if f is None:
+            f = self._fill[dtype] = torch.as_tensor(self._fill64, dtype=dtype, device=self.slot.device)
+        return f
+
+    def _check(self, t: torch.Tensor, n: int, name: str) -> torch.Tensor:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{name} must be a tensor")
+        if t.numel() != n:
+            raise ValueError(f"{name} has {t.numel()} entries, expected {n}")
+        if t.device != self.slot.device:
+            raise ValueError(f"{name} is on {t.device}, the map on {self.slot.device}")
+        dtype_code(t.dtype)  # float32 / float64 only
+        return t.reshape(-1).contiguous()
+
+    # A map built on the host (device="cpu", for host-side model assembly)
+    # indexes host tensors directly; a map on a GPU runs the kernels.
     def to_free(self, full: torch.Tensor) -> torch.Tensor:
-        return full.reshape(-1)[self.free_indices]
+        full = self._check(full, self.n_full, "full")
+        if not full.is_cuda:
+            return full[self.free_indices]
+        out = torch.empty(self.n_free, dtype=full.dtype, device=full.device)
+        _lib.call("agb_dof_to_free", dtype_code(full.dtype), self.n_free, ptr(self.free_indices), ptr(full),
+                  ptr(out), stream_ptr(full.device))
+        return out
 
     to_free_grad = to_free
     to_free_hess_diag = to_free
 
+    def _to_full(self, free: torch.Tensor, fill: bool) -> torch.Tensor:
+        free = self._check(free, self.n_free, "free")
+        f = self._fill_for(free.dtype) if fill else None
+        if not free.is_cuda:
+            out = f.clone() if f is not None else torch.zeros(self.n_full, dtype=free.dtype)
+            out[self.free_indices] = free
+            return out.reshape(self.n_points, self.dim)
+        out = torch.empty((self.n_points, self.dim), dtype=free.dtype, device=free.device)
+        _lib.call("agb_dof_to_full", dtype_code(free.dtype), self.n_full, ptr(self.slot), ptr(free), ptr(f), ptr(out),
+                  stream_ptr(free.device))
+        return out
+
     def to_full(self, free: torch.Tensor) -> torch.Tensor:
-        r = torch.empty(self.n_full, dtype=free.dtype, device=free.device)
-        r[self.fixed_indices] = self.fixed_values.to(free.dtype)
-        r[self.free_indices] = free
-        return r.reshape(self.n_points, self.dim)
+        return self._to_full(free, True)
 
     def to_full_grad(self, free: torch.Tensor) -> torch.Tensor:
-        r = torch.zeros(self.n_full, dtype=free.dtype, device=free.device)
-        r[self.free_indices] = free
-        return r.reshape(self.n_points, self.dim)
+        return self._to_full(free, False)
 
 
 class DofMapBuilder:

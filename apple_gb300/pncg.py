@@ -242,7 +242,7 @@ class PNCG:
         self.beta_max = beta_max
         # FP32 stable Neo-Hookean reference-state correction: refresh the FP64
         # reference gradient each time ||g|| drops by this factor; 0: off;
-        # < 0: on (1e-2) when rtol < 1e-5 asks for more than FP32 forces resolve
+        # < 0: on (0.1) when rtol < 1e-5 asks for more than FP32 forces resolve
         self.refresh_ratio = refresh_ratio
 
     def params(self, dtype) -> _lib.PncgParams:

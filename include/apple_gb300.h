@@ -185,6 +185,24 @@ int agb_model_destroy(agb_model* model);
 int agb_model_eval(agb_model* model, unsigned flags, const void* u, const void* p, double* energy,
                    void* grad, void* hess_diag, void* hess_prod, double* hess_quad, void* stream);
 
+/* Free/fixed DOF maps over the flattened n_points x 3 vector
+ * (DofMap.to_free / to_free_grad / to_free_hess_diag / to_full /
+ * to_full_grad, forward/dof_map/_dof_map.py:30-50), one kernel each, device
+ * pointers of the given precision.
+ *   agb_dof_to_free: free_out[i] = full[free_index[i]], i < n_free.
+ *   agb_dof_to_full: full_out[j] = slot[j] >= 0 ? free_in[slot[j]]
+ *                    : (fill ? fill[j] : 0), j < n_full; slot[j] is DOF j's
+ *                    free index or -1 for a fixed DOF.  fill = the fixed
+ *                    values scattered into a full-length vector gives
+ *                    to_full (:39-43); fill = NULL gives to_full_grad (:45-50).
+ * The indices are not checked on the device: free_index[i] < n_full and
+ * slot[j] < n_free are the caller's to keep (the Python DofMap builds both
+ * from one mask). */
+int agb_dof_to_free(int32_t precision, int64_t n_free, const int64_t* free_index, const void* full,
+                    void* free_out, void* stream);
+int agb_dof_to_full(int32_t precision, int64_t n_full, const int32_t* slot, const void* free_in,
+                    const void* fill, void* full_out, void* stream);
+
 /* ---------------------------------------------------------------------------
  * PNCG (liblaf-peach PNCG as used by forward/_forward.py:22-30; iteration as
  * benches/bench_pncg_branching_backends.py:254-456,606-679).
