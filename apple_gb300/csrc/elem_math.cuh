@@ -333,17 +333,49 @@ __device__ __forceinline__ double rsqrt_<double>(double x) {
   return rsqrt(x);
 }
 
+// Quotients whose last bits only steer the iteration: in FP32 the fast
+// division (__fdividef, within 2 ulp) and x * rsqrt(x) for x >= 1.  A Jacobi
+// rotation stays orthogonal whatever its angle (c = 1 / sqrt(1 + t^2),
+// s = t c), so the angle's rounding changes how fast the sweeps converge,
+// not the orthogonality of V.
+template <class R>
+__device__ __forceinline__ R quick_div(R a, R b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float quick_div<float>(float a, float b) {
+  return __fdividef(a, b);
+}
+template <class R>
+__device__ __forceinline__ R sqrt_ge1(R x) {  // x >= 1
+  return sqrt(x);
+}
+template <>
+__device__ __forceinline__ float sqrt_ge1<float>(float x) {
+  return x * rsqrtf(x);
+}
+// sqrt for x >= 0 (the singular values sqrt(1 + e)): in FP32 x * rsqrt(x),
+// within a few ulp, and 0 at 0
+template <class R>
+__device__ __forceinline__ R sqrt_ge0(R x) {
+  return sqrt(x);
+}
+template <>
+__device__ __forceinline__ float sqrt_ge0<float>(float x) {
+  return x > 0.0f ? x * rsqrtf(x) : 0.0f;
+}
+
 template <class R>
 __device__ __forceinline__ void jacobi_rotate(R (&A)[3][3], R (&V)[3][3], int p, int q) {
   const R apq = A[p][q];
   if (apq == R(0)) return;
-  const R theta = (A[q][q] - A[p][p]) / (R(2) * apq);
+  const R theta = quick_div(A[q][q] - A[p][p], R(2) * apq);
   const R at = fabs(theta);
   R t;
   if (at > R(1e15))
-    t = R(0.5) / theta;
+    t = quick_div(R(0.5), theta);
   else
-    t = (theta >= R(0) ? R(1) : R(-1)) / (at + sqrt(theta * theta + R(1)));
+    t = quick_div(theta >= R(0) ? R(1) : R(-1), at + sqrt_ge1(theta * theta + R(1)));
   const R c = rsqrt_(t * t + R(1));
   const R sn = t * c;
   A[p][p] -= t * apq;
@@ -476,13 +508,13 @@ __device__ void svd_rv(const R (&G)[3][3], R jm1, Svd<R>& out) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const R ei = fmax(e[i], R(-1));
-    const R si = sqrt(R(1) + ei);
+    const R si = sqrt_ge0(R(1) + ei);
     if (i == 2 && inverted) {
       out.s[i] = -si;
       out.sm1[i] = -si - R(1);
     } else {
       out.s[i] = si;
-      out.sm1[i] = ei / (si + R(1));
+      out.sm1[i] = quick_div(ei, si + R(1));
     }
   }
 }
@@ -507,9 +539,9 @@ __device__ __forceinline__ void arap_pk1(const Svd<R>& d, R mu, R (&P)[3][3]) {
 // (func/_misc.py:31-43, clamp on)
 template <class R>
 __device__ __forceinline__ void arap_lambdas(const Svd<R>& d, R (&l)[3]) {
-  l[0] = R(2) / fmax(d.s[0] + d.s[1], R(2));
-  l[1] = R(2) / fmax(d.s[1] + d.s[2], R(2));
-  l[2] = R(2) / fmax(d.s[2] + d.s[0], R(2));
+  l[0] = quick_div(R(2), fmax(d.s[0] + d.s[1], R(2)));
+  l[1] = quick_div(R(2), fmax(d.s[1] + d.s[2], R(2)));
+  l[2] = quick_div(R(2), fmax(d.s[2] + d.s[0], R(2)));
 }
 
 // Q_k : M for the twist modes of func/_misc.py:56-70 via W = U^T M V:
@@ -638,31 +670,21 @@ __device__ __forceinline__ void quat_of_rotation(const R (&M)[3][3], R (&q)[4]) 
   const R tx = R(1) + M[0][0] - M[1][1] - M[2][2];
   const R ty = R(1) - M[0][0] + M[1][1] - M[2][2];
   const R tz = R(1) - M[0][0] - M[1][1] + M[2][2];
-  if (tw >= tx && tw >= ty && tw >= tz) {
-    const R r = rsqrt_(tw), h = R(0.5) * r;
-    q[0] = R(0.5) * tw * r;
-    q[1] = (M[2][1] - M[1][2]) * h;
-    q[2] = (M[0][2] - M[2][0]) * h;
-    q[3] = (M[1][0] - M[0][1]) * h;
-  } else if (tx >= ty && tx >= tz) {
-    const R r = rsqrt_(tx), h = R(0.5) * r;
-    q[0] = (M[2][1] - M[1][2]) * h;
-    q[1] = R(0.5) * tx * r;
-    q[2] = (M[0][1] + M[1][0]) * h;
-    q[3] = (M[0][2] + M[2][0]) * h;
-  } else if (ty >= tz) {
-    const R r = rsqrt_(ty), h = R(0.5) * r;
-    q[0] = (M[0][2] - M[2][0]) * h;
-    q[1] = (M[0][1] + M[1][0]) * h;
-    q[2] = R(0.5) * ty * r;
-    q[3] = (M[1][2] + M[2][1]) * h;
-  } else {
-    const R r = rsqrt_(tz), h = R(0.5) * r;
-    q[0] = (M[1][0] - M[0][1]) * h;
-    q[1] = (M[0][2] + M[2][0]) * h;
-    q[2] = (M[1][2] + M[2][1]) * h;
-    q[3] = R(0.5) * tz * r;
-  }
+  // 4wx, 4wy, 4wz, 4xy, 4xz, 4yz
+  const R dx = M[2][1] - M[1][2], dy = M[0][2] - M[2][0], dz = M[1][0] - M[0][1];
+  const R sxy = M[0][1] + M[1][0], sxz = M[0][2] + M[2][0], syz = M[1][2] + M[2][1];
+  // the largest of 4w^2, 4x^2, 4y^2, 4z^2 (first of equals in w, x, y, z
+  // order); each component is (its product with that one, times 4) / (4
+  // sqrt(t)), selected without branches so that a warp does not diverge
+  const bool cw = tw >= tx && tw >= ty && tw >= tz;
+  const bool cx = !cw && tx >= ty && tx >= tz;
+  const bool cy = !cw && !cx && ty >= tz;
+  const R t = cw ? tw : (cx ? tx : (cy ? ty : tz));
+  const R h = R(0.5) * rsqrt_(t);
+  q[0] = h * (cw ? t : (cx ? dx : (cy ? dy : dz)));
+  q[1] = h * (cw ? dx : (cx ? t : (cy ? sxy : sxz)));
+  q[2] = h * (cw ? dy : (cx ? sxy : (cy ? t : syz)));
+  q[3] = h * (cw ? dz : (cx ? sxz : (cy ? syz : t)));
 }
 
 // the rotation of q / |q| (a stored quaternion is unit only to rounding):
