@@ -24,9 +24,10 @@ from .pncg import PNCG, Solution
 
 
 class BatchedForward:
-    """``models``: :class:`apple_gb300.model.Model` objects of one dtype with
-    stable Neo-Hookean or muscle potentials (with any muscle in the batch,
-    every cell runs as a muscle cell, the plain ones with zero activation).
+    """``models``: :class:`apple_gb300.model.Model` objects of one dtype and
+    one material family: ARAP potentials, or stable Neo-Hookean and muscle
+    potentials (with any muscle in the batch, every cell runs as a muscle
+    cell, the plain ones with zero activation).
     ``solve()`` minimises every model's energy from its current state (zero
     free displacement, fixed values applied)."""
 

@@ -29,7 +29,8 @@ constexpr int kTailThreads = 256;
 template <class R, int MAT>
 __global__ void __launch_bounds__(kElemThreads) batch_dir_kernel(BatchArgs b) {
   constexpr int N = 6;
-  constexpr unsigned FF = 0x2u;  // float-float warp tree for c2 (terms of both signs)
+  // float-float warp tree for c2 (terms of both signs); ARAP sums p^T H p only
+  constexpr unsigned FF = snh_family(MAT) ? 0x2u : 0x0u;
   __shared__ V4<R> sx[kTileVerts];
   __shared__ V4<R> sp[kTileVerts];
   __shared__ Acc<R> red[kWarps * N];
@@ -47,24 +48,35 @@ __global__ void __launch_bounds__(kElemThreads) batch_dir_kernel(BatchArgs b) {
   __syncthreads();
   Acc<R> sums[N] = {};
   const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  const V4<R>* csvd = MAT == AGB_ARAP ? svd_cache<R>(a, st->sbuf) : nullptr;
   for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
     ElemGeo<R> geo;
     uint32_t ids;
     load_elem_m<R, MAT>(a.fv, e, geo, ids);
     const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
-    R G[3][3], dF[3][3];
-    vec_gradient(sx, l, geo.D, G);
-    add_act<MAT>(geo, G);
+    R dF[3][3];
     vec_gradient(sp, l, geo.D, dF);
-    SnhPoint<R> s;
-    snh_prepare(G, s);
-    SnhDir<R> d;
-    snh_dir(s, dF, d);
-    sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
-    R c[5];
-    snh_poly(s, d, geo.mu, geo.lam, c);
+    if constexpr (snh_family(MAT)) {
+      R G[3][3];
+      vec_gradient(sx, l, geo.D, G);
+      add_act<MAT>(geo, G);
+      SnhPoint<R> s;
+      snh_prepare(G, s);
+      SnhDir<R> d;
+      snh_dir(s, dF, d);
+      sums[0].add(fmax(snh_hess_quad(s, d, geo.mu, geo.lam), R(0)));
+      R c[5];
+      snh_poly(s, d, geo.mu, geo.lam, c);
 #pragma unroll
-    for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
+      for (int m = 0; m < 5; ++m) sums[1 + m].add(c[m]);
+    } else {
+      // the SVD at x, kept by the gradient pass that evaluated x
+      Svd<R> sv;
+      svd_get(csvd, (size_t)a.fv.n_cells, e, sv);
+      R lk[3];
+      arap_lambdas(sv, lk);
+      sums[0].add(fmax(arap_hess_quad(sv, lk, dF, geo.mu), R(0)));
+    }
   }
   block_reduce<N, FF, R>(sums, red);
   if (threadIdx.x == 0) {
@@ -73,7 +85,7 @@ __global__ void __launch_bounds__(kElemThreads) batch_dir_kernel(BatchArgs b) {
   }
 }
 
-template <class R>
+template <class R, int MAT>
 __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs b) {
   constexpr int N = 6;
   __shared__ Acc<R> red[(kTailThreads / 32) * N];
@@ -93,17 +105,84 @@ __global__ void __launch_bounds__(kTailThreads) batch_dir_tail_kernel(BatchArgs 
     double tot[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) tot[k] = s[k].value();
-    dir_decide<AGB_STABLE_NEO_HOOKEAN>(st, tot);
+    dir_decide<MAT>(st, tot);
   }
 }
 
-template <class R, int MAT, bool DELTA>
-__global__ void __launch_bounds__(kGradThreads, 6) batch_grad_kernel(BatchArgs b) {
-  grad_tile<R, MAT, DELTA>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x]);
+// ARAP: the gradient pass at the first trial step x + alpha_0 p of each
+// tile's mesh (grad_tile's speculative form), its energy remainders summed
+// per tile
+template <class R>
+__global__ void __launch_bounds__(kGradThreads, 4) batch_grad_spec_kernel(BatchArgs b) {
+  __shared__ Acc<R> red[kGradWarps];
+  Acc<R> rem[1] = {};
+  const int tile = blockIdx.x;
+  if (!grad_tile<R, AGB_ARAP, false, true>(b.a, tile, b.st + b.tile_mesh[tile], &rem[0])) return;
+  block_reduce<1, 0x1u, R>(rem, red);
+  if (threadIdx.x == 0) ((AccStore<R>*)b.part_grad)[tile] = acc_store(rem[0]);
 }
 
+// ARAP: per mesh, the Armijo test of alpha_0 from its tiles' remainders
+template <class R>
+__global__ void __launch_bounds__(kTailThreads) batch_spec_tail_kernel(BatchArgs b) {
+  __shared__ Acc<R> red[kTailThreads / 32];
+  pdl_trigger();
+  pdl_wait();
+  SolverState* st = b.st + blockIdx.x;
+  if (st->done) return;
+  const int t0 = b.mesh_tile0[blockIdx.x], t1 = b.mesh_tile0[blockIdx.x + 1];
+  const double rem = block_sum_partials<R>((const AccStore<R>*)b.part_grad + t0, t1 - t0, 1, red);
+  if (threadIdx.x == 0) spec_decide(st, rem);
+}
+
+// ARAP: trial remainders at alpha_0 2^-j, j = j0 .. j0+nt-1, per tile of a
+// mesh whose step is not decided yet (three per tile into part_dir)
+template <class R>
+__global__ void __launch_bounds__(kElemThreads) batch_trial_kernel(BatchArgs b, int j0, int nt) {
+  __shared__ Acc<R> red[kWarps * 3];
+  const int tile = blockIdx.x;
+  const SolverState* st = b.st + b.tile_mesh[tile];
+  if (st->done || st->decided) return;
+  Acc<R> sums[3] = {};
+  trial_tile<R>(b.a, tile, st, j0, nt, sums);
+  block_reduce<3, 0x7u, R>(sums, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ((AccStore<R>*)b.part_dir)[(size_t)tile * 6 + j] = acc_store(sums[j]);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kTailThreads) batch_trial_tail_kernel(BatchArgs b, int j0, int nt) {
+  __shared__ Acc<R> red[(kTailThreads / 32) * 3];
+  SolverState* st = b.st + blockIdx.x;
+  if (st->done || st->decided) return;
+  const int t0 = b.mesh_tile0[blockIdx.x], t1 = b.mesh_tile0[blockIdx.x + 1];
+  Acc<R> s[3] = {};
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) s[j].add(acc_load<R>((const AccStore<R>*)b.part_dir + (size_t)t * 6 + j));
+  }
+  block_reduce<3, 0xffffffffu, R>(s, red);
+  if (threadIdx.x == 0) {
+    double tot[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) tot[j] = s[j].value();
+    trial_decide(st, st->alpha0, j0, nt, tot);
+  }
+}
+
+// fallback (ARAP): the pass after the trial passes, for the meshes whose
+// speculative step was rejected
+template <class R, int MAT, bool DELTA>
+__global__ void __launch_bounds__(kGradThreads, 6) batch_grad_kernel(BatchArgs b, int fallback) {
+  grad_tile<R, MAT, DELTA>(b.a, blockIdx.x, b.st + b.tile_mesh[blockIdx.x], nullptr, fallback != 0);
+}
+
+// phase (ARAP): 1 after the speculative gradient pass, for the meshes whose
+// alpha_0 was accepted; 2 after the fallback passes, for the others; 0: all
 template <class R, bool DELTA>
-__global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
+__global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b, int phase) {
   constexpr int N = 12;
   constexpr unsigned FF = (1u << 1) | (1u << 6) | (1u << 8) | (1u << 9);
   __shared__ Acc<R> red[(kVThreads / 32) * N];
@@ -114,6 +193,7 @@ __global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
   pdl_trigger();
   pdl_wait();
   if (st->done) return;
+  if ((phase == 1 && !st->spec_ok) || (phase == 2 && st->spec_ok)) return;
   const R t = (R)st->t;
   const V4<R>* P = p_cur<R>(a, st->pbuf);
   R s[N] = {};
@@ -131,15 +211,21 @@ __global__ void __launch_bounds__(kVThreads) batch_vertex_kernel(BatchArgs b) {
   }
 }
 
+// phase as in batch_vertex_kernel; the pass of phase 1 decides its meshes
+// only, the others also count the meshes still running
 template <class R>
-__global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchArgs b) {
+__global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchArgs b, int phase) {
   constexpr int N = 12;
   __shared__ Acc<R> red[(kTailThreads / 32) * N];
   __shared__ bool s_last;
   pdl_wait();
   SolverState* st = b.st + blockIdx.x;
-  const bool was_done = st->done != 0;  // read by every thread before thread 0 writes it
-  if (!was_done) {
+  // read by every thread before thread 0 writes the state
+  const bool was_done = st->done != 0;
+  const bool mine = phase == 0 || (phase == 1) == (st->spec_ok != 0);
+  __syncthreads();
+  if (phase == 1 && !mine) return;
+  if (!was_done && mine) {
     const int c0 = b.mesh_chunk0[blockIdx.x], c1 = b.mesh_chunk0[blockIdx.x + 1];
     Acc<R> s[N] = {};
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
@@ -152,8 +238,10 @@ __global__ void __launch_bounds__(kTailThreads) batch_vertex_tail_kernel(BatchAr
 #pragma unroll
       for (int k = 0; k < N; ++k) tot[k] = s[k].value();
       vertex_decide(st, tot);
+      if (b.a.svd) st->sbuf ^= 1;  // the gradient pass's SVDs are those at the new x
     }
   }
+  if (phase == 1) return;
   if (threadIdx.x == 0) {
     if (!st->done) atomicAdd(&b.bs->n_active, 1u);
     __threadfence();
@@ -254,6 +342,8 @@ __global__ void batch_init_state_kernel(BatchArgs b, SolverState proto) {
     st.pbuf = 0;
     st.refresh = 0;
     st.gnorm_ref = 0.0;
+    st.sbuf = 0;
+    st.spec_ok = 0;
     b.st[m] = st;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *b.bs = BatchState{0, 0, 0u, 0u};
@@ -288,12 +378,14 @@ cudaError_t batch_refresh(const BatchArgs& b, cudaStream_t s) {
 }
 
 template <class R, int MAT, bool DELTA>
-cudaError_t batch_grad_and_vertex_d(const BatchArgs& b, cudaStream_t s) {
+cudaError_t batch_grad_and_vertex_d(const BatchArgs& b, cudaStream_t s, int fallback = 0) {
+  const int phase = fallback ? 2 : 0;
   cudaError_t e = launch_pdl_b(batch_grad_kernel<R, MAT, DELTA>, dim3(b.a.fv.n_tiles), dim3(kGradThreads),
-                               grad_smem_bytes<R>(), s, b);
-  if (e == cudaSuccess) e = launch_pdl_b(batch_vertex_kernel<R, DELTA>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b);
+                               grad_smem_bytes<R>(), s, b, fallback);
   if (e == cudaSuccess)
-    e = launch_pdl_b(batch_vertex_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+    e = launch_pdl_b(batch_vertex_kernel<R, DELTA>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b, phase);
+  if (e == cudaSuccess)
+    e = launch_pdl_b(batch_vertex_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b, phase);
   if (e == cudaSuccess && DELTA) e = batch_refresh(b, s);
   return e;
 }
@@ -309,6 +401,7 @@ cudaError_t batch_grad_and_vertex_m(const BatchArgs& b, cudaStream_t s) {
 
 template <class R>
 cudaError_t batch_grad_and_vertex(const BatchArgs& b, cudaStream_t s) {
+  if (b.a.fv.material == AGB_ARAP) return batch_grad_and_vertex_d<R, AGB_ARAP, false>(b, s);
   return b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE
              ? batch_grad_and_vertex_m<R, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(b, s)
              : batch_grad_and_vertex_m<R, AGB_STABLE_NEO_HOOKEAN>(b, s);
@@ -318,13 +411,43 @@ template <class R, int MAT>
 cudaError_t batch_iteration_m(const BatchArgs& b, cudaStream_t s) {
   batch_dir_kernel<R, MAT><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = launch_pdl_b(batch_dir_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  if (e == cudaSuccess)
+    e = launch_pdl_b(batch_dir_tail_kernel<R, MAT>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
   if (e == cudaSuccess) e = batch_grad_and_vertex_m<R, MAT>(b, s);
+  return e;
+}
+
+// ARAP: the speculative gradient pass at alpha_0 and its vertex pass for the
+// meshes that accept it; for the others the trial passes (three halvings
+// each), then the gradient and vertex passes at the step they decide.  Every
+// pass returns at once for a mesh it does not concern.
+template <class R>
+cudaError_t batch_iteration_arap(const BatchArgs& b, cudaStream_t s) {
+  constexpr int A = AGB_ARAP;
+  const int nt = b.a.fv.n_tiles, max_bt = b.a.max_bt;
+  batch_dir_kernel<R, A><<<nt, kElemThreads, 0, s>>>(b);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_pdl_b(batch_dir_tail_kernel<R, A>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  if (e == cudaSuccess)
+    e = launch_pdl_b(batch_grad_spec_kernel<R>, dim3(nt), dim3(kGradThreads), grad_spec_smem_bytes<R>(), s, b);
+  if (e == cudaSuccess) e = launch_pdl_b(batch_spec_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b);
+  if (e == cudaSuccess)
+    e = launch_pdl_b(batch_vertex_kernel<R, false>, dim3(b.n_chunks), dim3(kVThreads), 0, s, b, 1);
+  if (e == cudaSuccess)
+    e = launch_pdl_b(batch_vertex_tail_kernel<R>, dim3(b.n_meshes), dim3(kTailThreads), 0, s, b, 1);
+  for (int j0 = 1; e == cudaSuccess && j0 <= max_bt; j0 += 3) {
+    const int k = max_bt - j0 + 1 < 3 ? max_bt - j0 + 1 : 3;
+    batch_trial_kernel<R><<<nt, kElemThreads, 0, s>>>(b, j0, k);
+    batch_trial_tail_kernel<R><<<b.n_meshes, kTailThreads, 0, s>>>(b, j0, k);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = batch_grad_and_vertex_d<R, A, false>(b, s, 1);
   return e;
 }
 
 template <class R>
 cudaError_t batch_iteration_t(const BatchArgs& b, cudaStream_t s) {
+  if (b.a.fv.material == AGB_ARAP) return batch_iteration_arap<R>(b, s);
   return b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE ? batch_iteration_m<R, AGB_STABLE_NEO_HOOKEAN_MUSCLE>(b, s)
                                                           : batch_iteration_m<R, AGB_STABLE_NEO_HOOKEAN>(b, s);
 }
@@ -335,6 +458,8 @@ cudaError_t batch_prepare_t() {
   const int g = (int)grad_smem_bytes<R>();
   constexpr int SNH = AGB_STABLE_NEO_HOOKEAN, MU = AGB_STABLE_NEO_HOOKEAN_MUSCLE;
   cudaError_t e = cudaFuncSetAttribute(batch_grad_kernel<R, SNH, false>, m, g);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_grad_kernel<R, AGB_ARAP, false>, m, g);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_grad_spec_kernel<R>, m, (int)grad_spec_smem_bytes<R>());
   if (e == cudaSuccess && kRefDelta<R, SNH>) e = cudaFuncSetAttribute(batch_grad_kernel<R, SNH, kRefDelta<R, SNH>>, m, g);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_grad_kernel<R, MU, false>, m, g);
   if (e == cudaSuccess && kRefDelta<R, MU>) e = cudaFuncSetAttribute(batch_grad_kernel<R, MU, kRefDelta<R, MU>>, m, g);
@@ -385,14 +510,19 @@ cudaError_t launch_batch_set_limit(const BatchArgs& b, int n, cudaStream_t s) {
 cudaError_t launch_batch_energy(const BatchArgs& b, cudaStream_t s) {
   if (b.n_meshes == 0) return cudaSuccess;
   const bool mu = b.a.fv.material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+  const bool arap = b.a.fv.material == AGB_ARAP;
   if (b.a.precision == AGB_F64) {
-    if (mu)
+    if (arap)
+      batch_energy_pass_kernel<double, AGB_ARAP><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+    else if (mu)
       batch_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     else
       batch_energy_pass_kernel<double, AGB_STABLE_NEO_HOOKEAN><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     batch_energy_kernel<double><<<b.n_meshes, kTailThreads, 0, s>>>(b);
   } else {
-    if (mu)
+    if (arap)
+      batch_energy_pass_kernel<float, AGB_ARAP><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
+    else if (mu)
       batch_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN_MUSCLE><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);
     else
       batch_energy_pass_kernel<float, AGB_STABLE_NEO_HOOKEAN><<<b.a.fv.n_tiles, kElemThreads, 0, s>>>(b);

@@ -1457,7 +1457,7 @@ int agb_batch_destroy(agb_batch* b) {
                   (void*)b->d_slot_of_tv, (void*)b->d_off, (void*)b->d_uoi, b->d_fixed, b->d_force,
                   (void*)b->d_tile_mesh, (void*)b->d_mesh_tile0, (void*)b->d_chunk_v0, (void*)b->d_chunk_mesh,
                   (void*)b->d_mesh_chunk0, b->d_xa, b->d_gd, b->d_p0, b->d_p1, b->d_xref, b->d_gref, b->d_slots,
-                  b->d_part, b->d_act,
+                  b->d_svd, b->d_part, b->d_act,
                   (void*)b->d_state, (void*)b->d_bstate})
     dfree(p);
   if (b->h_state) cudaFreeHost(b->h_state);
@@ -1476,19 +1476,22 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
     AGB_REQUIRE(m && !m->fems.empty(), AGB_E_INVALID, "agb_batch_create: model %d has no FEM potential", k);
     AGB_REQUIRE(m->precision == prec, AGB_E_INVALID, "agb_batch_create: models must share a precision");
     int64_t n_cells = 0;
-    for (agb_fem* f : m->fems) {
-      AGB_REQUIRE(f->material == AGB_STABLE_NEO_HOOKEAN || f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE,
-                  AGB_E_INVALID, "agb_batch_create: the batched form runs stable Neo-Hookean and muscle potentials");
-      n_cells += f->plan.n_cells;
-    }
+    for (agb_fem* f : m->fems) n_cells += f->plan.n_cells;
     AGB_REQUIRE(n_cells > 0, AGB_E_INVALID, "agb_batch_create: model %d: its FEM potentials have no cells", k);
   }
-  // with any muscle potential every cell runs as a muscle cell (zero activation
-  // for the stable Neo-Hookean ones)
-  bool any_muscle = false;
+  // one material per batch, as per solver: ARAP, or stable Neo-Hookean and
+  // muscle potentials, where with any muscle every cell runs as a muscle cell
+  // (zero activation for the stable Neo-Hookean ones)
+  bool any_muscle = false, any_arap = false, any_snh = false;
   for (int k = 0; k < n_models; ++k)
-    for (agb_fem* f : models[k]->fems) any_muscle |= f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
-  const int bmat = any_muscle ? AGB_STABLE_NEO_HOOKEAN_MUSCLE : AGB_STABLE_NEO_HOOKEAN;
+    for (agb_fem* f : models[k]->fems) {
+      any_muscle |= f->material == AGB_STABLE_NEO_HOOKEAN_MUSCLE;
+      any_arap |= f->material == AGB_ARAP;
+      any_snh |= f->material == AGB_STABLE_NEO_HOOKEAN;
+    }
+  AGB_REQUIRE(!(any_arap && (any_snh || any_muscle)), AGB_E_INVALID,
+              "agb_batch_create: ARAP and stable Neo-Hookean potentials cannot share a batch");
+  const int bmat = any_arap ? AGB_ARAP : (any_muscle ? AGB_STABLE_NEO_HOOKEAN_MUSCLE : AGB_STABLE_NEO_HOOKEAN);
   agb_pncg_params prm;
   agb_pncg_default_params(&prm);
   if (params) prm = *params;
@@ -1497,7 +1500,7 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   if (chunk_verts <= 0) chunk_verts = 512;
   AGB_REQUIRE(prm.refresh_ratio < 1.0, AGB_E_INVALID, "agb_batch_create: bad parameters");
   if (prm.refresh_ratio < 0.0) prm.refresh_ratio = (prm.rtol < 1e-5 && prm.atol == 0.0) ? 1e-1 : 0.0;
-  const bool delta = prec == AGB_F32 && prm.refresh_ratio > 0.0;
+  const bool delta = prec == AGB_F32 && bmat != AGB_ARAP && prm.refresh_ratio > 0.0;
   agb_batch* b = new (std::nothrow) agb_batch();
   AGB_REQUIRE(b, AGB_E_INVALID, "agb_batch_create: out of host memory");
   b->models.assign(models, models + n_models);
@@ -1619,6 +1622,7 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   if (!rc && delta) rc = dalloc_bytes(&b->d_xref, v4 * np);
   if (!rc && delta) rc = dalloc_bytes(&b->d_gref, v4 * np);
   if (!rc) rc = dalloc_bytes(&b->d_slots, 2 * v4 * (size_t)b->n_slots);
+  if (!rc && bmat == AGB_ARAP) rc = dalloc_bytes(&b->d_svd, 2 * 3 * v4 * (size_t)P.n_cells);
   const size_t n_part = (size_t)P.n_tiles * 7 + (size_t)n_chunks * 12;
   if (!rc) rc = dalloc_bytes(&b->d_part, 8 * n_part);
   if (!rc) rc = dalloc(&b->d_state, (size_t)n_models);
@@ -1658,6 +1662,7 @@ int agb_batch_create(int32_t n_models, agb_model* const* models, const agb_pncg_
   a.off = b->d_off;
   a.slots = b->d_slots;
   a.n_slots = b->n_slots;
+  a.svd = b->d_svd;
   a.st = nullptr;
   a.max_bt = prm.max_backtracking;
   ba.n_meshes = n_models;

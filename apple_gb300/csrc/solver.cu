@@ -34,6 +34,7 @@
 // writes after it.
 #include <math.h>
 
+#include "bulk.cuh"
 #include "kernels.h"
 #include "solver.h"
 #include "solver_common.cuh"
@@ -62,8 +63,8 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   // float-float warp trees only for c2 (terms of both signs); p^T H p is a
   // sum of clamped non-negative terms, c3..c6 are higher-order corrections
   constexpr unsigned FF = snh_family(MAT) ? 0x2u : 0x0u;
-  __shared__ V4<R> sx[kTileVerts];
-  __shared__ V4<R> sp[kTileVerts];
+  __shared__ V4<R> sxp[kTileVerts];  // (x, p.x)
+  __shared__ V2<R> sq[kTileVerts];   // (p.y, p.z)
   __shared__ Acc<R> red[kWarps * N];
   SolverState* st = a.st;
   pdl_trigger();
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   R plain[N] = {};
   Acc<R> c2acc = {};
   for (; tile < a.fv.n_tiles; tile += gridDim.x) {
-    stage_dir<R>(a, vid, beta, inv_mean, pprev, pcur, sx, sp);
+    stage_dir_packed<R>(a, vid, beta, inv_mean, pprev, pcur, sxp, sq);
     // the next tile's vertex id, in flight while this tile computes
     vid = tile_vertex(a.fv, tile + gridDim.x, threadIdx.x);
     __syncthreads();
@@ -115,9 +116,8 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
       if (last ? en < een : true) load_elem_m<R, MAT>(a.fv, en, geon, idsn);
       const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
       R G[3][3], dF[3][3];
-      vec_gradient(sx, l, geo.D, G);
+      dir_gradients(sxp, sq, l, geo.D, G, dF);
       add_act<MAT>(geo, G);
-      vec_gradient(sp, l, geo.D, dF);
       if constexpr (snh_family(MAT)) {
         SnhPoint<R> s;
         snh_prepare(G, s);
@@ -172,74 +172,18 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
 // ---------------------------------------------------------------------------
 template <class R>
 __global__ void __launch_bounds__(kElemThreads) solver_trial_kernel(SolveArgs a, int j0, int nt) {
-  __shared__ R sh[3][kTileVerts];
-  __shared__ R sl[3][kTileVerts];
-  __shared__ R sp[3][kTileVerts];
   __shared__ Acc<R> red[kWarps * 3];
   SolverState* st = a.st;
   if (st->done || st->decided) return;
   const double a0 = st->alpha0;
-  R tj[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) tj[j] = (R)ldexp(a0, -(j0 + j));
-  const int tile = blockIdx.x;
-  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
-  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
-  stage_direction<R>(a, vs, nv, p_cur<R>(a, st->pbuf), sh, sl, sp);
-  const V4<R>* cbase = svd_cache<R>(a, st->sbuf);
-  __syncthreads();
   Acc<R> sums[3] = {};
-  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
-    ElemGeo<R> geo;
-    uint32_t ids;
-    load_elem<R>(a.fv, e, geo, ids);
-    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
-    R w[4][3], G[3][3], dF[3][3];
-    position_gradient(sh, sl, l, geo.D, G);
-    gather_corners(sp, l, w);
-    corner_gradient(w, geo.D, dF);
-    Svd<R> base;
-    svd_get(cbase, (size_t)a.fv.n_cells, e, base);
-#pragma unroll 1
-    for (int j = 0; j < nt; ++j) {
-      R Gt[3][3];
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) Gt[i][k] = fma_rn(tj[j], dF[i][k], G[i][k]);
-      Svd<R> trial;
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) trial.V[i][k] = base.V[i][k];
-      svd_rv<R, true>(Gt, (Gt[0][0] + Gt[1][1] + Gt[2][2]) + inv2(Gt) + det3(Gt), trial);
-      sums[j].add(arap_remainder(base, trial, tj[j], dF, geo.mu));
-    }
-  }
+  trial_tile<R>(a, blockIdx.x, st, j0, nt, sums);
   double tot[3];
   if (!grid_reduce2<3, 0x7u, R>(sums, (AccStore<R>*)a.part_t, (AccStore<R>*)a.gpart_t, a.cnt_t,
                                 gridDim.x, red, tot))
     return;
   if (threadIdx.x != 0) return;
-  const double gd = st->gd;
-  for (int j = 0; j < nt; ++j) {
-    const int J = j0 + j;
-    if (J > st->max_bt) break;
-    const double t = ldexp(a0, -J);
-    const double de = gd * t + tot[j];
-    if (isfinite(de) && de <= st->armijo_c * t * gd) {
-      st->t = t;
-      st->delta_e = de;
-      st->ls_ok = 1;
-      st->ls_steps = J;
-      st->decided = 1;
-      return;
-    }
-  }
-  if (j0 + nt - 1 >= st->max_bt) {
-    reject_step(st, st->max_bt);
-    st->decided = 1;
-  }
+  trial_decide(st, a0, j0, nt, tot);
 }
 
 // ---------------------------------------------------------------------------
@@ -328,6 +272,174 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_ker
   if (threadIdx.x != 0) return;
   vertex_decide(st, tot);
   if (a.svd) st->sbuf ^= 1;  // the gradient pass's SVDs are those at the new x
+  const bool go = !st->done && st->iter < st->iter_limit;
+  if (use_cond)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
+                            (go && !(a.refresh_exits && st->refresh)) ? 1u : 0u);
+}
+
+// The FP32 vertex pass with its inputs streamed by bulk copies.  Each CTA
+// walks chunks of kVThreads consecutive vertices (chunk c = blockIdx.x + k *
+// gridDim.x, one vertex per thread: the vertex of each thread is the one the
+// grid-stride kernel above gives it, so the sums and results are the same
+// bits).  Thread 0 copies a chunk's positions, gradient/diagonal, direction,
+// reference gradient, force and its contiguous range of slots into shared
+// memory with cp.async.bulk, one chunk ahead (two stages, one mbarrier
+// each), so the loads of a chunk are in flight while the one before it
+// computes and no thread waits on a dependent global load.  Slots beyond the
+// stage's capacity are read from global memory.
+constexpr int kVSlotCap = 768;  // slots staged per chunk
+constexpr size_t kVsXa = 0;
+constexpr size_t kVsGd = kVsXa + (size_t)kVThreads * 32;
+constexpr size_t kVsP = kVsGd + (size_t)kVThreads * 32;
+constexpr size_t kVsR = kVsP + (size_t)kVThreads * 16;
+constexpr size_t kVsF = kVsR + (size_t)kVThreads * 16;
+constexpr size_t kVsS = kVsF + (size_t)kVThreads * 16;
+constexpr size_t kVStage = kVsS + (size_t)kVSlotCap * 32;
+constexpr size_t kVBulkSmem = 2 * kVStage;
+
+template <bool DELTA>
+__global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_bulk_kernel(SolveArgs a, int use_cond,
+                                                                                        int phase) {
+  using R = float;
+  constexpr int N = 12;
+  extern __shared__ __align__(128) unsigned char vsm[];
+  __shared__ Acc<R> red[(kVThreads / 32) * N];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int s_base[2];  // first slot of the chunk in each stage
+  const int n = a.n_points, tid = threadIdx.x;
+  const int nchunks = (n + kVThreads - 1) / kVThreads;
+  int c = blockIdx.x;
+  // constant inputs before the dependency wait: this thread's slot range in
+  // its first chunk, and thread 0's chunk bounds for the first two chunks
+  int s0 = 0, s1 = 0;
+  if (c * kVThreads + tid < n) {
+    s0 = a.off[c * kVThreads + tid];
+    s1 = a.off[c * kVThreads + tid + 1];
+  }
+  int blo[2] = {0, 0}, bhi[2] = {0, 0};
+  if (tid == 0) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int cc = c + j * gridDim.x;
+      if (cc < nchunks) {
+        blo[j] = a.off[cc * kVThreads];
+        bhi[j] = a.off[min(cc * kVThreads + kVThreads, n)];
+      }
+    }
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  pdl_wait();
+  SolverState* st = a.st;
+  if (st->done) {
+    if (use_cond && blockIdx.x == 0 && tid == 0) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, 0u);
+    return;
+  }
+  if (guard_skip(a, st)) return;
+  if ((phase == 1 && !st->spec_ok) || (phase == 2 && st->spec_ok)) return;
+  const R t = (R)st->t;
+  const V4<R>* P = p_cur<R>(a, st->pbuf);
+  const V4<R>* XA = (const V4<R>*)a.xa;
+  const V4<R>* GD = (const V4<R>*)a.gd;
+  const V4<R>* GR = (const V4<R>*)a.gref;
+  const V4<R>* FO = (const V4<R>*)a.force;
+  const V4<R>* SL = (const V4<R>*)a.slots;
+  // thread 0: copy chunk cc (slot range [lo, hi)) into `stage`
+  auto issue = [&](int cc, int stage, int lo, int hi) {
+    const int v0 = cc * kVThreads, cnt = min(kVThreads, n - v0);
+    const int ns = min(hi - lo, kVSlotCap);
+    unsigned char* b = vsm + (size_t)stage * kVStage;
+    const uint32_t vb = 16u * (uint32_t)cnt;
+    // positions and gradient/diagonal 32 B per vertex, direction (and the
+    // reference gradient, the force) 16 B, slots 32 B
+    const uint32_t bytes = 5u * vb + (DELTA ? vb : 0u) + (FO ? vb : 0u) + 32u * (uint32_t)ns;
+    s_base[stage] = lo;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[stage], bytes);
+    bulk_g2s(b + kVsXa, XA + 2 * (size_t)v0, 2 * vb, &bar[stage]);
+    bulk_g2s(b + kVsGd, GD + 2 * (size_t)v0, 2 * vb, &bar[stage]);
+    bulk_g2s(b + kVsP, P + v0, vb, &bar[stage]);
+    if (DELTA) bulk_g2s(b + kVsR, GR + v0, vb, &bar[stage]);
+    if (FO) bulk_g2s(b + kVsF, FO + v0, vb, &bar[stage]);
+    if (ns > 0) bulk_g2s(b + kVsS, SL + 2 * (size_t)lo, 32u * (uint32_t)ns, &bar[stage]);
+  };
+  if (tid == 0 && c < nchunks) issue(c, 0, blo[0], bhi[0]);
+  __syncthreads();
+  // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
+  R s[N] = {};
+  bool bad = false;
+  for (int k = 0; c < nchunks; c += gridDim.x, ++k) {
+    const int stage = k & 1;
+    const int cn = c + gridDim.x;
+    if (tid == 0 && cn < nchunks) {
+      issue(cn, stage ^ 1, blo[1], bhi[1]);
+      // bounds of the chunk after it, for the next issue
+      const int c2 = cn + gridDim.x;
+      if (c2 < nchunks) {
+        blo[1] = a.off[c2 * kVThreads];
+        bhi[1] = a.off[min(c2 * kVThreads + kVThreads, n)];
+      }
+    }
+    // this thread's slot range in the next chunk
+    int s0n = 0, s1n = 0;
+    const int in_next = cn * kVThreads + tid;
+    if (cn < nchunks && in_next < n) {
+      s0n = a.off[in_next];
+      s1n = a.off[in_next + 1];
+    }
+    if (!mbar_wait(&bar[stage], (uint32_t)(k >> 1) & 1u)) bad = true;
+    const int i = c * kVThreads + tid;
+    if (i < n && !bad) {
+      const unsigned char* b = vsm + (size_t)stage * kVStage;
+      VertexIn<R> in;
+      in.x = ((const V4<R>*)(b + kVsXa))[2 * tid];
+      in.xl = ((const V4<R>*)(b + kVsXa))[2 * tid + 1];
+      in.g = ((const V4<R>*)(b + kVsGd))[2 * tid];
+      in.p = ((const V4<R>*)(b + kVsP))[tid];
+      if (DELTA) in.r = ((const V4<R>*)(b + kVsR))[tid];
+      if (FO) in.f = ((const V4<R>*)(b + kVsF))[tid];
+      in.s0 = s0;
+      in.s1 = s1;
+      const V4<R>* ss = (const V4<R>*)(b + kVsS);
+      const int base = s_base[stage];
+      R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
+      for (int q = s0; q < s1; ++q) {
+        const int j = q - base;
+        const V4<R> sg = j < kVSlotCap ? ss[2 * j] : SL[2 * (size_t)q];
+        const V4<R> sd = j < kVSlotCap ? ss[2 * j + 1] : SL[2 * (size_t)q + 1];
+        gs[0] += sg.x;
+        gs[1] += sg.y;
+        gs[2] += sg.z;
+        ds[0] += sd.x;
+        ds[1] += sd.y;
+        ds[2] += sd.z;
+      }
+      vertex_apply<R, DELTA>(a, i, in, t, gs, ds, s);
+    }
+    s0 = s0n;
+    s1 = s1n;
+    __syncthreads();  // this stage is read before it is refilled
+  }
+  if (bad) atomicMax(&st->error, 2);  // a copy never completed: the solve stops with a device error
+  double tot[N];
+  constexpr unsigned FF = (1u << 1) | (1u << 6) | (1u << 8) | (1u << 9);
+  Acc<R> acc[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    acc[k] = Acc<R>{};
+    acc[k].add(s[k]);
+  }
+  if (!grid_reduce_masked<N, FF, R>(acc, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
+  if (tid != 0) return;
+  if (st->error) {
+    st->done = 1;
+  } else {
+    vertex_decide(st, tot);
+    if (a.svd) st->sbuf ^= 1;
+  }
   const bool go = !st->done && st->iter < st->iter_limit;
   if (use_cond)
     cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
@@ -467,6 +579,10 @@ static cudaError_t prepare_t() {
   constexpr int MU = AGB_STABLE_NEO_HOOKEAN_MUSCLE;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_grad_kernel<R, MU, false>, m, g);
   if (e == cudaSuccess && kRefDelta<R, MU>) e = cudaFuncSetAttribute(solver_grad_kernel<R, MU, kRefDelta<R, MU>>, m, g);
+  if constexpr (sizeof(R) == 4) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_vertex_bulk_kernel<false>, m, (int)kVBulkSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(solver_vertex_bulk_kernel<true>, m, (int)kVBulkSmem);
+  }
   return e;
 }
 
@@ -532,6 +648,17 @@ static cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t sme
   return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
+// the vertex pass as a programmatic dependent: FP32 streams its inputs with
+// bulk copies, FP64 uses the grid-stride kernel
+template <class R, bool DELTA>
+static cudaError_t launch_vertex(const SolveArgs& a, int use_cond, int phase, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4)
+    return launch_pdl(solver_vertex_bulk_kernel<DELTA>, dim3(a.vblocks), dim3(kVThreads), kVBulkSmem, s, a,
+                      use_cond, phase);
+  else
+    return launch_pdl(solver_vertex_kernel<R, DELTA>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond, phase);
+}
+
 template <class R, int MAT, bool DELTA>
 static cudaError_t launch_iteration_d(const SolveArgs& a, bool use_cond, bool first, int max_bt,
                                       cudaStream_t s) {
@@ -554,18 +681,18 @@ static cudaError_t launch_iteration_d(const SolveArgs& a, bool use_cond, bool fi
       const dim3 gb(kGradThreads), vg(a.vblocks), vb(kVThreads);
       const int uc = use_cond ? 1 : 0;
       cudaError_t e = launch_pdl(solver_grad_spec_kernel<R>, eg, gb, grad_spec_smem_bytes<R>(), s, a);
-      if (e == cudaSuccess) e = launch_pdl(solver_vertex_kernel<R, DELTA>, vg, vb, 0, s, a, uc, 1);
+      if (e == cudaSuccess) e = launch_vertex<R, DELTA>(a, uc, 1, s);
       if (e != cudaSuccess) return e;
       for (int j0 = 1; j0 <= max_bt; j0 += 3)
         solver_trial_kernel<R><<<eg, eb, 0, s>>>(a, j0, max_bt - j0 + 1 < 3 ? max_bt - j0 + 1 : 3);
       e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, gb, grad_smem_bytes<R>(), s, a, 1);
       if (e != cudaSuccess) return e;
-      return launch_pdl(solver_vertex_kernel<R, DELTA>, vg, vb, 0, s, a, uc, 2);
+      return launch_vertex<R, DELTA>(a, uc, 2, s);
     }
   }
   cudaError_t e = launch_pdl(solver_grad_kernel<R, MAT, DELTA>, eg, dim3(kGradThreads), grad_smem_bytes<R>(), s, a, 0);
   if (e != cudaSuccess) return e;
-  return launch_pdl(solver_vertex_kernel<R, DELTA>, dim3(a.vblocks), dim3(kVThreads), 0, s, a, use_cond ? 1 : 0, 0);
+  return launch_vertex<R, DELTA>(a, use_cond ? 1 : 0, 0, s);
 }
 
 template <class R, int MAT>
@@ -612,7 +739,12 @@ static cudaError_t launch_pass_d(const SolveArgs& a, int which, cudaStream_t s) 
     else
       solver_grad_kernel<R, MAT, DELTA><<<eg, kGradThreads, grad_smem_bytes<R>(), s>>>(a, 0);
   }
-  if (which == 2) solver_vertex_kernel<R, DELTA><<<a.vblocks, kVThreads, 0, s>>>(a, 0, 0);
+  if (which == 2) {
+    if constexpr (sizeof(R) == 4)
+      solver_vertex_bulk_kernel<DELTA><<<a.vblocks, kVThreads, kVBulkSmem, s>>>(a, 0, 0);
+    else
+      solver_vertex_kernel<R, DELTA><<<a.vblocks, kVThreads, 0, s>>>(a, 0, 0);
+  }
   return cudaGetLastError();
 }
 

@@ -304,6 +304,7 @@ struct agb_batch {
   void* d_xref = nullptr;  // reference state (FP32)
   void* d_gref = nullptr;
   void* d_slots = nullptr;
+  void* d_svd = nullptr;   // ARAP: the two per-element SVD caches
   void* d_part = nullptr;
   agb::SolverState* d_state = nullptr;
   agb::SolverState* h_state = nullptr;  // pinned, n_meshes

@@ -162,6 +162,43 @@ __device__ __forceinline__ void stage_dir(const SolveArgs& a, int v, R beta, R i
   sp[threadIdx.x] = pv;
 }
 
+// the same, staged as 24 bytes per vertex: (x, p.x) and (p.y, p.z), so that
+// a corner of both fields is one 16-byte and one 8-byte shared-memory load
+template <class R>
+__device__ __forceinline__ void stage_dir_packed(const SolveArgs& a, int v, R beta, R inv_mean,
+                                                 const V4<R>* pprev, V4<R>* pcur, V4<R>* sxp, V2<R>* sq) {
+  if (v < 0) return;
+  const V4<R> x = ldg4((const V4<R>*)a.xa + 2 * v), g = ldg4((const V4<R>*)a.gd + 2 * v),
+              d = ldg4((const V4<R>*)a.gd + 2 * v + 1), po = ldg4(pprev + v);
+  R p[3];
+  pdir(g, d, po, beta, inv_mean, p);
+  pcur[v] = V4<R>{p[0], p[1], p[2], R(0)};
+  sxp[threadIdx.x] = V4<R>{x.x, x.y, x.z, p[0]};
+  sq[threadIdx.x] = V2<R>{p[1], p[2]};
+}
+
+// G = sum_a (x_a - x_0) D_a^T and dF = sum_a (p_a - p_0) D_a^T from the
+// packed staging (the same arithmetic as vec_gradient on each field)
+template <class R>
+__device__ __forceinline__ void dir_gradients(const V4<R>* sxp, const V2<R>* sq, const int (&l)[4],
+                                              const R (&D)[3][3], R (&G)[3][3], R (&dF)[3][3]) {
+  const V4<R> w0 = sxp[l[0]], w1 = sxp[l[1]], w2 = sxp[l[2]], w3 = sxp[l[3]];
+  const V2<R> q0 = sq[l[0]], q1 = sq[l[1]], q2 = sq[l[2]], q3 = sq[l[3]];
+  const R e[3][3] = {{w1.x - w0.x, w2.x - w0.x, w3.x - w0.x},
+                     {w1.y - w0.y, w2.y - w0.y, w3.y - w0.y},
+                     {w1.z - w0.z, w2.z - w0.z, w3.z - w0.z}};
+  const R f[3][3] = {{w1.w - w0.w, w2.w - w0.w, w3.w - w0.w},
+                     {q1.x - q0.x, q2.x - q0.x, q3.x - q0.x},
+                     {q1.y - q0.y, q2.y - q0.y, q3.y - q0.y}};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      G[i][j] = e[i][0] * D[0][j] + e[i][1] * D[1][j] + e[i][2] * D[2][j];
+      dF[i][j] = f[i][0] * D[0][j] + f[i][1] * D[1][j] + f[i][2] * D[2][j];
+    }
+}
+
 // the thread's vertex of a tile, or -1
 __device__ __forceinline__ int tile_vertex(const FemView& fv, int tile, int i) {
   if (tile >= fv.n_tiles) return -1;
@@ -315,6 +352,77 @@ __device__ __forceinline__ void spec_decide(SolverState* st, double rem) {
   }
 }
 
+// ARAP trial pass over one tile (kElemThreads threads): each element's
+// remainder at the trial steps alpha_0 2^-j, j = j0 .. j0+nt-1 (nt <= 3),
+// into sums[j]; each trial SVD is warm-started from the cached one at x
+template <class R>
+__device__ __forceinline__ void trial_tile(const SolveArgs& a, int tile, const SolverState* st, int j0, int nt,
+                                           Acc<R> (&sums)[3]) {
+  __shared__ R sh[3][kTileVerts];
+  __shared__ R sl[3][kTileVerts];
+  __shared__ R sp[3][kTileVerts];
+  const double a0 = st->alpha0;
+  R tj[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) tj[j] = (R)ldexp(a0, -(j0 + j));
+  const int vs = a.fv.tile_vstart[tile], nv = a.fv.tile_vstart[tile + 1] - vs;
+  const int es = a.fv.tile_estart[tile], ee = a.fv.tile_estart[tile + 1];
+  stage_direction<R>(a, vs, nv, p_cur<R>(a, st->pbuf), sh, sl, sp);
+  const V4<R>* cbase = svd_cache<R>(a, st->sbuf);
+  __syncthreads();
+  for (int e = es + threadIdx.x; e < ee; e += blockDim.x) {
+    ElemGeo<R> geo;
+    uint32_t ids;
+    load_elem<R>(a.fv, e, geo, ids);
+    const int l[4] = {corner(ids, 0), corner(ids, 1), corner(ids, 2), corner(ids, 3)};
+    R w[4][3], G[3][3], dF[3][3];
+    position_gradient(sh, sl, l, geo.D, G);
+    gather_corners(sp, l, w);
+    corner_gradient(w, geo.D, dF);
+    Svd<R> base;
+    svd_get(cbase, (size_t)a.fv.n_cells, e, base);
+#pragma unroll 1
+    for (int j = 0; j < nt; ++j) {
+      R Gt[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Gt[i][k] = fma_rn(tj[j], dF[i][k], G[i][k]);
+      Svd<R> trial;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) trial.V[i][k] = base.V[i][k];
+      svd_rv<R, true>(Gt, (Gt[0][0] + Gt[1][1] + Gt[2][2]) + inv2(Gt) + det3(Gt), trial);
+      sums[j].add(arap_remainder(base, trial, tj[j], dF, geo.mu));
+    }
+  }
+}
+
+// thread 0 after the trial sums tot[j] of steps alpha_0 2^-(j0 + j): the
+// reference's Armijo test, in order; after the last halving a rejection
+__device__ __forceinline__ void trial_decide(SolverState* st, double a0, int j0, int nt, const double* tot) {
+  const double gd = st->gd;
+  for (int j = 0; j < nt; ++j) {
+    const int J = j0 + j;
+    if (J > st->max_bt) break;
+    const double t = ldexp(a0, -J);
+    const double de = gd * t + tot[j];
+    if (isfinite(de) && de <= st->armijo_c * t * gd) {
+      st->t = t;
+      st->delta_e = de;
+      st->ls_ok = 1;
+      st->ls_steps = J;
+      st->decided = 1;
+      return;
+    }
+  }
+  if (j0 + nt - 1 >= st->max_bt) {
+    reject_step(st, st->max_bt);
+    st->decided = 1;
+  }
+}
+
 // Last block of the vertex pass (thread 0): Dai-Kou beta, preconditioner
 // mean, descent check and termination from the 12 sums
 // 0 gPg 1 gPy 2 yPy 3 sum|d| 4 count 5 zgg 6 zgy 7 zyy 8 y.p 9 p.g 10 g.g 11 ext energy
@@ -400,29 +508,19 @@ __device__ __forceinline__ void vertex_load(const SolveArgs& a, int i, int s0, i
   in.s1 = s1;
 }
 
+// the rest of a vertex once its slots are summed (gs, ds in slot order)
 template <class R, bool DELTA>
-__device__ __forceinline__ void vertex_finish(const SolveArgs& a, int i, const VertexIn<R>& in, R t,
-                                              R (&s)[12]) {
+__device__ __forceinline__ void vertex_apply(const SolveArgs& a, int i, const VertexIn<R>& in, R t,
+                                             R (&gs)[3], const R (&ds)[3], R (&s)[12]) {
   V4<R>* XA = (V4<R>*)a.xa;
   V4<R>* GD = (V4<R>*)a.gd;
   const bool ext = a.force != nullptr;
-  const V4<R>* slots = (const V4<R>*)a.slots;
   const int mask = (int)in.x.w;
   const R p[3] = {in.p.x, in.p.y, in.p.z};
   R xh[3] = {in.x.x, in.x.y, in.x.z}, xlo[3] = {in.xl.x, in.xl.y, in.xl.z};
 #pragma unroll
   for (int c = 0; c < 3; ++c) pair_add(xh[c], xlo[c], mul_rn(t, p[c]));
   const R xn[3] = {xh[0] + xlo[0], xh[1] + xlo[1], xh[2] + xlo[2]};
-  R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
-  for (int k = in.s0; k < in.s1; ++k) {
-    const V4<R> sg = slots[2 * k], sd = slots[2 * k + 1];
-    gs[0] += sg.x;
-    gs[1] += sg.y;
-    gs[2] += sg.z;
-    ds[0] += sd.x;
-    ds[1] += sd.y;
-    ds[2] += sd.z;
-  }
   if constexpr (DELTA) {
     // g = g(x_ref) + sum_e (f_e(x) - f_e(x_ref)); the force is folded into g(x_ref)
     gs[0] += in.r.x;
@@ -465,6 +563,23 @@ __device__ __forceinline__ void vertex_finish(const SolveArgs& a, int i, const V
   XA[2 * i + 1] = V4<R>{xlo[0], xlo[1], xlo[2], R(0)};
   GD[2 * i] = V4<R>{gn[0], gn[1], gn[2], R(0)};
   GD[2 * i + 1] = V4<R>{dn[0], dn[1], dn[2], R(0)};
+}
+
+template <class R, bool DELTA>
+__device__ __forceinline__ void vertex_finish(const SolveArgs& a, int i, const VertexIn<R>& in, R t,
+                                              R (&s)[12]) {
+  const V4<R>* slots = (const V4<R>*)a.slots;
+  R gs[3] = {R(0), R(0), R(0)}, ds[3] = {R(0), R(0), R(0)};
+  for (int k = in.s0; k < in.s1; ++k) {
+    const V4<R> sg = slots[2 * k], sd = slots[2 * k + 1];
+    gs[0] += sg.x;
+    gs[1] += sg.y;
+    gs[2] += sg.z;
+    ds[0] += sd.x;
+    ds[1] += sd.y;
+    ds[2] += sd.z;
+  }
+  vertex_apply<R, DELTA>(a, i, in, t, gs, ds, s);
 }
 
 template <class R, bool DELTA>
