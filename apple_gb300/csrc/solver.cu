@@ -198,9 +198,13 @@ size_t solver_grad_smem(int precision) {
   return precision == AGB_F64 ? grad_smem_bytes<double>() : grad_smem_bytes<float>();
 }
 
+// The tiles run in reverse order: the direction pass before this one walks
+// them forward, so its last tiles' element records are the ones most likely
+// still in L2 when this pass starts (the result does not depend on the
+// order: each tile writes its own slots).
 template <class R, int MAT, bool DELTA>
 __global__ void __launch_bounds__(kGradThreads, 5) solver_grad_kernel(SolveArgs a, int fallback) {
-  grad_tile<R, MAT, DELTA>(a, blockIdx.x, a.st, nullptr, fallback != 0);
+  grad_tile<R, MAT, DELTA>(a, gridDim.x - 1 - blockIdx.x, a.st, nullptr, fallback != 0);
 }
 
 // ARAP: the gradient pass at the first trial step x + alpha_0 p, with the
