@@ -319,9 +319,10 @@ int agb_solver_time_passes(agb_solver* solver, int32_t reps, void* flush, size_t
 int agb_pncg_minimize_host(agb_solver* solver, void* u_host, agb_pncg_stats* stats, void* stream);
 
 /* ---------------------------------------------------------------------------
- * Batched PNCG: independent models (each its own space, stable Neo-Hookean
- * or muscle potentials of one precision with at least one cell, fixed DOFs,
- * external force) solved together.
+ * Batched PNCG: independent models (each its own space, potentials of one
+ * precision with at least one cell, fixed DOFs, external force) solved
+ * together.  The models' FEM potentials are all ARAP, or all stable
+ * Neo-Hookean and muscle (AGB_E_INVALID otherwise, as for one solver).
  * Every model runs the PNCG iteration above with its own beta, step and
  * termination; an iteration of all running models is one set of launches
  * (one CUDA graph).  No reference counterpart: the reference steps one
