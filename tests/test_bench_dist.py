@@ -69,3 +69,27 @@ def test_reference_arm_nonzero_rank_does_no_work(monkeypatch, capsys):
 
     bench.run_reference(A())
     assert not called and capsys.readouterr().out == ""
+
+
+def test_reference_arm_prints_the_gpu_arms_config(monkeypatch, capsys):
+    """The reference arm's line names the same workload configuration as the
+    GPU arm's (headline_config), so that the two lines compare like for like."""
+    sys.path.insert(0, ROOT)
+    import json
+
+    import bench
+
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setattr(bench, "cpu_reference", lambda *a, **k: {
+        "value": 30.0, "unit": "iter/s", "cores": 16, "kind": "port", "sample": "stub", "iters": 3, "warmup": 1})
+
+    class A:
+        steps, warmup, cpu_budget, small, gpus = 3, 1, 1.0, False, 1
+
+    bench.run_reference(A())
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["config"] == bench.headline_config(False, 1)
+    assert line["config"]["n_tets"] == 1_500_000 and line["config"]["n_vertices"] == 314_721
+    assert line["metric"] == bench.METRIC and line["unit"] == "iter/s" and line["higher_is_better"]
