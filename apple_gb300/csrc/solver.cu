@@ -739,7 +739,7 @@ static cudaError_t launch_iteration(const SolveArgs& a, bool use_cond, bool firs
 
 template <class R, int MAT, bool DELTA>
 static cudaError_t launch_pass_d(const SolveArgs& a, int which, cudaStream_t s) {
-  const dim3 eg(a.fv.n_tiles), eb(kElemThreads);
+  const dim3 eg(a.fv.n_tiles);
   if (which == 0) launch_dir<R, MAT>(a, 0, false, s);
   if (which == 1) {
     if constexpr (MAT == AGB_ARAP)  // the iteration's gradient pass is the speculative one
