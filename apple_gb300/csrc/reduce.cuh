@@ -236,6 +236,49 @@ __device__ __forceinline__ bool grid_reduce_masked(Acc<R> (&a)[N], AccStore<R>* 
   return true;
 }
 
+// grid_reduce_masked, and the last block also copies `words` 32-bit words of
+// `src` (the solver's scalar state) into shared `dst` in the same round trip
+// as the partials, so that its scalar logic reads shared memory instead of
+// making one dependent global load per field.  `dst` is complete in every
+// thread of the last block on return.
+template <int N, unsigned FF, class R>
+__device__ __forceinline__ bool grid_reduce_masked_state(Acc<R> (&a)[N], AccStore<R>* partials,
+                                                         unsigned* counter, int nblocks, Acc<R>* scratch,
+                                                         double (&total)[N], const uint32_t* src,
+                                                         uint32_t* dst, int words) {
+  __shared__ bool s_last;
+  block_reduce<N, FF, R>(a, scratch);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) partials[(size_t)blockIdx.x * N + k] = acc_store(a[k]);
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    s_last = (prev == (unsigned)nblocks - 1u);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  uint32_t w = 0;
+  if ((int)threadIdx.x < words) w = __ldcg(src + threadIdx.x);
+  Acc<R> b[N] = {};
+#pragma unroll 2
+  for (int blk = threadIdx.x; blk < nblocks; blk += blockDim.x) {
+    Acc<R> v[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = acc_load<R>(partials + (size_t)blk * N + k);
+#pragma unroll
+    for (int k = 0; k < N; ++k) b[k].add(v[k]);
+  }
+  if ((int)threadIdx.x < words) dst[threadIdx.x] = w;
+  block_reduce<N, 0xffffffffu, R>(b, scratch);  // ends with a barrier: dst is complete
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) total[k] = b[k].value();
+    *counter = 0u;
+  }
+  return true;
+}
+
 template <int N, class R>
 __device__ __forceinline__ bool grid_reduce(Acc<R> (&a)[N], AccStore<R>* partials, unsigned* counter,
                                             int nblocks, Acc<R>* scratch, double (&total)[N]) {

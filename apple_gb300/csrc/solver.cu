@@ -49,6 +49,11 @@ namespace agb {
 constexpr int kVertexCtasPerSM = 2;
 constexpr int kDirCtasPerSM = 3;
 
+// SolverState as 32-bit words, for the last blocks' shared copy
+constexpr int kStateWords = (int)(sizeof(SolverState) / 4);
+static_assert(sizeof(SolverState) % 4 == 0 && kStateWords <= kVThreads && kStateWords <= kElemThreads,
+              "the state is copied one word per thread");
+
 int solver_vertex_blocks(int n_points) {
   int b = (n_points + kVThreads - 1) / kVThreads;
   const int cap = kSMs * kVertexCtasPerSM;
@@ -66,6 +71,7 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
   __shared__ V4<R> sxp[kTileVerts];  // (x, p.x)
   __shared__ V2<R> sq[kTileVerts];   // (p.y, p.z)
   __shared__ Acc<R> red[kWarps * N];
+  __shared__ SolverState sst;
   SolverState* st = a.st;
   pdl_trigger();
   static_assert(kTileVerts == kElemThreads, "one staged vertex per thread");
@@ -158,9 +164,13 @@ __global__ void __launch_bounds__(kElemThreads, kDirCtasPerSM) solver_dir_kernel
     sums[k].add(plain[k]);
   }
   if constexpr (N > 1) sums[1] = c2acc;
-  if (!grid_reduce_masked<N, FF, R>(sums, (AccStore<R>*)a.part_a, a.cnt_a, gridDim.x, red, tot)) return;
-  if (threadIdx.x != 0) return;
-  dir_decide<MAT>(st, tot);
+  // the last block decides on a shared copy of the state (see the vertex pass)
+  if (!grid_reduce_masked_state<N, FF, R>(sums, (AccStore<R>*)a.part_a, a.cnt_a, gridDim.x, red, tot,
+                                          (const uint32_t*)st, (uint32_t*)&sst, kStateWords))
+    return;
+  if (threadIdx.x == 0) dir_decide<MAT>(&sst, tot);
+  __syncthreads();
+  if ((int)threadIdx.x < kStateWords) ((uint32_t*)st)[threadIdx.x] = ((const uint32_t*)&sst)[threadIdx.x];
 }
 
 // ---------------------------------------------------------------------------
@@ -311,6 +321,7 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_bul
   __shared__ Acc<R> red[(kVThreads / 32) * N];
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ int s_base[2];  // first slot of the chunk in each stage
+  __shared__ SolverState sst;
   const int n = a.n_points, tid = threadIdx.x;
   const int nchunks = (n + kVThreads - 1) / kVThreads;
   int c = blockIdx.x;
@@ -436,18 +447,25 @@ __global__ void __launch_bounds__(kVThreads, kVertexCtasPerSM) solver_vertex_bul
     acc[k] = Acc<R>{};
     acc[k].add(s[k]);
   }
-  if (!grid_reduce_masked<N, FF, R>(acc, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot)) return;
-  if (tid != 0) return;
-  if (st->error) {
-    st->done = 1;
-  } else {
-    vertex_decide(st, tot);
-    if (a.svd) st->sbuf ^= 1;
+  // the last block decides on a shared copy of the state, loaded with the
+  // block partials, and writes it back in one coalesced store
+  if (!grid_reduce_masked_state<N, FF, R>(acc, (AccStore<R>*)a.part_v, a.cnt_v, gridDim.x, red, tot,
+                                          (const uint32_t*)st, (uint32_t*)&sst, kStateWords))
+    return;
+  if (tid == 0) {
+    if (sst.error) {
+      sst.done = 1;
+    } else {
+      vertex_decide(&sst, tot);
+      if (a.svd) sst.sbuf ^= 1;
+    }
+    const bool go = !sst.done && sst.iter < sst.iter_limit;
+    if (use_cond)
+      cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
+                              (go && !(a.refresh_exits && sst.refresh)) ? 1u : 0u);
   }
-  const bool go = !st->done && st->iter < st->iter_limit;
-  if (use_cond)
-    cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond,
-                            (go && !(a.refresh_exits && st->refresh)) ? 1u : 0u);
+  __syncthreads();
+  if (tid < kStateWords) ((uint32_t*)st)[tid] = ((const uint32_t*)&sst)[tid];
 }
 
 // total energy at x, on demand: an element pass into per-tile partials, then
