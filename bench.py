@@ -688,7 +688,7 @@ def run_ours(a) -> None:
         if rec.get("workload") == WORKLOAD:
             traffic = rec.get(names[k])
 
-    # the spec solve: PNCG from the initial state to ||g||/||g0|| <= 1e-6
+    # the headline solve: PNCG from the initial state to ||g||/||g0|| <= 1e-6
     solve_opt = ag.PNCG(ag.ConvergenceCriteria(max_steps=20000, rtol=1e-6))
     solve_sv = solve_opt.solver(ag.ForwardProblem(model))
     solve_sv.reset(u0)
